@@ -1,0 +1,329 @@
+"""ptnee throughput benchmark (Mpaths/s) on the 1M-triangle procedural scene.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step renders one full frame of the workload: the seeded 1M-triangle
+terrain + spheres scene, 1920x1080, 64 samples per pixel, max depth 8,
+Russian roulette from depth 3, Philox seed 0 (132.7 M camera paths). The
+scene (BVH, triangles, materials) and the path state live in HBM; both are
+larger than the 129 MB L2 (about 150 MB of scene and 380 MB of path state
+per wavefront batch), so no L2 flush is inserted between steps.
+
+value: paths / s with the scene resident and the image left on the device
+(nr_render with no host output), timed with CUDA events on the library's
+stream. e2e: the same render through nr_render with a pinned host output
+image, so the 24.9 MB device-to-host copy is inside the timed region.
+
+Multi-GPU (torchrun): every rank renders its own 64-sample range of the
+frame (sample0 = 64 * rank) with no collective on the data path (weak
+scaling); timing takes the max over ranks.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement in oracle/ (bit-identical to the reference on x86; the
+reference sources themselves are not present on the GPU host), all threads,
+on a bounded pixel sample of the same workload per step.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED = os.path.join(ROOT, "MEASURED_PEAKS.json")
+BYTES_NODE = 64      # one internal node: both child boxes + references
+BYTES_TRI = 48       # one triangle: p0, e1, e2 (+ ids)
+BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry, material type
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--res", default="1920x1080")
+    ap.add_argument("--wave", type=int, default=0, help="paths per wavefront batch (0: library default)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-tile-stride", type=int, default=32, help="CPU sample: every k-th 4x4 tile")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    from nuray_gb300 import scenes
+    sc = scenes.terrain_spheres(0)
+    w, h = (int(x) for x in args.res.split("x"))
+    params = sc["params"].replace("imgw=1920", f"imgw={w}").replace("imgh=1080", f"imgh={h}")
+    params = params.replace("spp=64", f"spp={args.spp}")
+    if args.wave:
+        params += f" wave={args.wave}"
+    desc = (f"procedural terrain+spheres, {sc['pos'].shape[0]} triangles, {w}x{h}, spp={args.spp}, "
+            "maxdepth 8, RR from depth 3, GGX-reflect materials, 32 quad lights, Philox seed 0")
+    return sc, params, desc, w, h
+
+
+def peaks():
+    try:
+        return json.load(open(MEASURED)), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0:
+                    self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_sample_pixels(w, h, stride):
+    tiles = [(x, y) for y in range(0, h, 4) for x in range(0, w, 4)]
+    pix = []
+    for k, (x0, y0) in enumerate(tiles):
+        if k % stride == 0:
+            pix += [(x, y) for y in range(y0, min(h, y0 + 4)) for x in range(x0, min(w, x0 + 4))]
+    return np.array(pix, np.int32)
+
+
+def cpu_leg(sc, params, spp, w, h, stride, budget_s=20.0):
+    """The oracle restatement on all host threads over a pixel sample; returns
+    (Mpaths/s, description, threads)."""
+    from oracle.bind import Oracle
+    P = Oracle("port", sc)
+    threads = os.cpu_count() or 1
+    pix = cpu_sample_pixels(w, h, stride)
+    # calibrate on a small slice, then size the timed sample to the budget
+    probe = pix[:: max(1, len(pix) // 256)]
+    t = time.perf_counter()
+    P.render_samples(params, probe, spp, threads=threads)
+    rate = len(probe) * spp / max(1e-6, time.perf_counter() - t)
+    n = int(min(len(pix), max(64, budget_s * rate / spp)))
+    pix = pix[:n]
+    t = time.perf_counter()
+    P.render_samples(params, pix, spp, threads=threads)
+    dt = time.perf_counter() - t
+    desc = (f"{n} pixels (every {stride}th 4x4 tile, first {n}) x {spp} spp of the same frame, "
+            f"{n * spp} paths in {dt:.1f} s")
+    return n * spp / dt / 1e6, desc, threads
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference algorithm on the host cores."""
+    if rank != 0:
+        return
+    sc, params, desc, w, h = workload(args)
+    from oracle.bind import Oracle
+    P = Oracle("port", sc)
+    threads = os.cpu_count() or 1
+    pix = cpu_sample_pixels(w, h, 256)
+    spp = args.spp
+    for _ in range(args.warmup):
+        P.render_samples(params, pix[:16], spp, threads=threads)
+    t = time.perf_counter()
+    for k in range(args.steps):
+        P.render_samples(params, pix, spp, sample0=spp * k, threads=threads)
+    dt = time.perf_counter() - t
+    v = len(pix) * spp * args.steps / dt / 1e6
+    sample = f"{len(pix)} pixels (every 256th 4x4 tile) x {spp} spp per step"
+    out = {"impl": "reference", "metric": "Mpaths/s ptnee", "value": round(v, 4), "unit": "Mpaths/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+           "config": {"workload": desc, "host_threads": threads},
+           "cpu_baseline": {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from nuray_gb300 import Scene, build
+    build.build()
+    sc, params, desc, w, h = workload(args)
+    t0 = time.perf_counter()
+    S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"])
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(S.stream())
+    spp = args.spp
+    base = params + f" sample0={spp * rank}"
+
+    # untimed instrumented frame: traversal work per ray for the roofline bytes
+    S.render_device(base.replace(f"spp={spp}", "spp=1") + " count=1")
+    cnt = S.stats()
+    for _ in range(args.warmup):
+        S.render_device(base + " profile=1")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    trace_ms, trace_launches, rays, shadow_rays, launches = 0.0, 0, 0, 0, 0
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for k in range(args.steps):
+            S.render_device(base + " profile=1")
+            st = S.stats()
+            trace_ms += st["kernel_ms_trace"]
+            trace_launches += st["trace_launches"]
+            rays += st["rays"]
+            shadow_rays += st["shadow_rays"]
+            launches += st["kernel_launches"]
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    paths_total = float(w * h * spp * args.steps * world)
+    value = paths_total / (ms / 1e3) / 1e6
+
+    # end to end through the C ABI with a pinned host image
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((h, w, 3), dtype=torch.float32, pin_memory=True)
+        hp = host.data_ptr()
+        from nuray_gb300._lib import check, lib
+        barrier()
+        t = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            check(lib().nr_render(S._h, None, base.encode(), ctypes.c_void_p(hp), None, None, None, None))
+        e1.record(stream)
+        e1.synchronize()
+        barrier()
+        ems = e0.elapsed_time(e1)
+        if dist is not None:
+            t2 = torch.tensor([ems], device="cuda")
+            dist.all_reduce(t2, op=dist.ReduceOp.MAX)
+            ems = float(t2.item())
+        e2e = {"value": round(paths_total / (ems / 1e3) / 1e6, 3), "unit": "Mpaths/s",
+               "h2d_bytes_per_step": len(base.encode()) + 44, "d2h_bytes_per_step": w * h * 3 * 4,
+               "ms_per_step": round(ems / args.steps, 2)}
+        launches_e2e = S.stats()["kernel_launches"] + 1
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    pk, pk_kind = peaks()
+    bytes_per_ray = (BYTES_NODE * cnt["nodes_visited"] + BYTES_TRI * cnt["tris_tested"]) / max(1, cnt["rays"]) \
+        + BYTES_RAY_IO
+    trace_bytes = bytes_per_ray * rays
+    achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
+    peak = pk.get("hbm_gbs", 6800.0)
+    roof = {"kernel": "k_trace (closest hit + material sort)", "bound": "hbm",
+            "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 3) if achieved else None, "peak_source": pk_kind,
+            "traffic": None,
+            "bytes_per_ray": round(bytes_per_ray, 1),
+            "nodes_per_ray": round(cnt["nodes_visited"] / max(1, cnt["rays"]), 2),
+            "tris_per_ray": round(cnt["tris_tested"] / max(1, cnt["rays"]), 2),
+            "avg_launch_ms": round(trace_ms / max(1, trace_launches), 4),
+            "share_of_step": round(trace_ms / ms, 3)}
+    traffic_file = os.path.join(ROOT, "profiles", "k_trace_traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            tr = json.load(open(traffic_file))
+            roof["traffic"] = round(tr["dram_bytes_per_ray"] * rays / max(1, trace_launches))
+            roof["traffic_note"] = tr.get("note")
+        except Exception:
+            pass
+
+    cpu = None
+    if not args.no_cpu and world == 1:
+        v, sample, threads = cpu_leg(sc, params, spp, w, h, args.cpu_tile_stride)
+        cpu = {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": sample}
+
+    out = {"metric": "Mpaths/s ptnee", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 2),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded procedural scene; the reference publishes no benchmark scene)",
+           "config": {"workload": desc, "triangles": int(sc["pos"].shape[0]), "paths_per_step": w * h * spp,
+                      "l2": "inputs larger than L2 (scene ~150 MB, path state ~380 MB per batch); no flush",
+                      "parallelism": f"{world} rank(s), disjoint sample ranges, no collective on the data path",
+                      "scene_build_s": round(build_s, 2)},
+           "rays_per_s": round((rays + shadow_rays) / (ms / 1e3), 1), "extension_rays": rays,
+           "shadow_rays": shadow_rays, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+           "e2e": e2e, "clocks": clk.summary()}
+    if e2e:
+        out["gpu_launches_e2e"] = launches_e2e * args.steps
+    print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/* nuray.h — C ABI of libnuray_gpu.so, the GB300 (sm_103a) implementation of
+ * nuRay's `ptnee` renderer (RendererPTLS, src/renderer/rendererptls.cpp).
+ *
+ * Every entry point returns an int status: NR_OK (0) or a negative NR_ERR_*
+ * code. No C++ exception crosses this boundary. The message of the last
+ * error on the calling thread is available from nr_last_error().
+ *
+ * Threading: calls on one scene are serialised by the library (one CUDA
+ * stream and one lock per scene); distinct scenes may be used from
+ * different threads. All pointers are host pointers unless a flag says
+ * otherwise.
+ *
+ * Reference interfaces replaced (file:line in the reference project):
+ *   nr_scene_load / nr_scene_create  Loader::fromSceneDescription (src/scene/loader.cpp:26-108)
+ *                                    + Renderer::prepare (src/renderer/renderer.cpp:30-39)
+ *   nr_scene_destroy                 Loader::~Loader / BVH::~BVH (src/scene/loader.cpp:10-16,
+ *                                    src/hierarchy/bvh.cpp:76-79)
+ *   nr_intersect                     Renderer::intersect -> BVH::intersection
+ *                                    (src/renderer/renderer.cpp:10-28, src/hierarchy/bvh.cpp:129-137)
+ *   nr_camera_from_params            Camera(fov, asp, pos, yaw, pitch, roll) as built by Cmd::main
+ *                                    (src/cmd/cmd.cpp:99-101, src/scene/camera.cpp:16-22,88-105)
+ *   nr_render                        RendererPTLS::render (src/renderer/rendererptls.cpp:96-236)
+ *   nr_render_samples                the per-sample loop body of RendererPTLS::render
+ *                                    (src/renderer/rendererptls.cpp:170-174) for listed pixels
+ *   nr_material_probe                Material::bxdf/pdf/sampleBxdf (src/material/material.h:7-24)
+ *   nr_get_stats / nr_scene_stream   no reference counterpart (the reference reports only a
+ *                                    wall-clock "secs used", src/renderer/rendererptls.cpp:232-233)
+ */
+#ifndef NURAY_H
+#define NURAY_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NR_OK 0
+#define NR_ERR_INVALID (-1)    /* bad argument, malformed scene or parameter */
+#define NR_ERR_CUDA (-2)       /* a CUDA call failed */
+#define NR_ERR_OOM (-3)        /* device or host allocation failed */
+#define NR_ERR_CANCELLED (-4)  /* *cancel became 0 during nr_render */
+#define NR_ERR_IO (-5)         /* a scene file could not be read */
+#define NR_ERR_DEVICE (-6)     /* a kernel reported an internal error (stack overflow, bad index) */
+
+/* Material types: the reference's Material subclasses (src/material/). */
+#define NR_MAT_LAMBERT 0     /* MatLambert    (src/material/matlambert.cpp) */
+#define NR_MAT_GGXR 1        /* MatGGXRefl    (src/material/matggxrefl.cpp), -m=ggxr */
+#define NR_MAT_GGX 2         /* MatGGX        (src/material/matggx.cpp), -m=ggx dielectric */
+#define NR_MAT_GLASS 3       /* MatGlass      (src/material/matglass.cpp), -m=glass */
+#define NR_MAT_BLINNPHONG 4  /* MatBlinnPhong (src/material/matblinnphong.cpp), MTL Ks>0 */
+#define NR_MAT_LIGHT 5       /* MatLight      (src/material/matlight.cpp), MTL Ke>0 or -m=light */
+
+/* One material, 64 bytes.
+ *   c0: Kd (Lambert, GGXR, GGX, BlinnPhong), F0 (Glass) or Ke (Light)
+ *   c1: Ks (BlinnPhong)
+ *   alpha: GGX roughness; ior: GGX / Glass index; ns: BlinnPhong exponent
+ *   tex0: texture index replacing c0 (map_Kd, glass map_F0), -1 for none
+ *   tex1: texture index replacing c1 (map_Ks), -1 for none */
+typedef struct nr_material {
+    int32_t type;
+    int32_t tex0;
+    int32_t tex1;
+    int32_t reserved0;
+    float c0[3];
+    float c1[3];
+    float alpha;
+    float ior;
+    float ns;
+    float reserved1[3];
+} nr_material;
+
+/* A flattened scene, in the reference Loader's triangle order.
+ *   pos: 9 floats per triangle (p0, p1, p2)
+ *   uv:  6 floats per triangle (t0.xy, t1.xy, t2.xy), may be NULL (zeros)
+ *   nrm: 9 floats per triangle (n0, n1, n2), may be NULL; as in the
+ *        reference's Triangle constructor a face normal replaces them
+ *        when |n0|^2 < 1e-4 (src/scene/triangle.cpp:12-25)
+ *   mat: material index per triangle
+ *   textures: tex_wh holds (width, height) per texture, tex_data the
+ *        concatenated linear RGB floats, row-major, row 0 at v = 1
+ *   env_tex: texture index of the environment map or -1; env_gain its gain
+ * The library copies everything; the caller's buffers may be freed after
+ * nr_scene_create returns. */
+typedef struct nr_scene_desc {
+    int32_t num_tris;
+    const float* pos;
+    const float* uv;
+    const float* nrm;
+    const int32_t* mat;
+    int32_t num_mats;
+    const nr_material* mats;
+    int32_t num_tex;
+    const int32_t* tex_wh;
+    const float* tex_data;
+    int32_t env_tex;
+    float env_gain;
+} nr_scene_desc;
+
+/* Pinhole camera (struct Camera, src/scene/camera.h:6-31). fov is the
+ * vertical field of view in degrees, aspect = film width / height. */
+typedef struct nr_camera {
+    float pos[3];
+    float gaze[3];
+    float up[3];
+    float fov;
+    float aspect;
+} nr_camera;
+
+typedef struct nr_scene nr_scene;
+
+/* Render statistics of the last nr_render / nr_render_samples on a scene. */
+/* Render statistics of the last nr_render / nr_render_samples on a scene.
+ * Kernel times are filled when the parameters contain profile=1 (CUDA events
+ * around every kernel of the wavefront), traversal counts when they contain
+ * count=1 (instrumented traversal kernels, slower). */
+typedef struct nr_stats {
+    uint64_t paths;            /* camera samples traced */
+    uint64_t rays;             /* extension rays (camera + continuation) */
+    uint64_t shadow_rays;      /* NEE shadow rays */
+    uint64_t waves;            /* wavefront batches */
+    uint64_t bounces;          /* trace/shade iterations over all waves */
+    uint64_t kernel_launches;  /* kernels launched by the call */
+    uint64_t trace_launches;   /* of which closest-hit traversal */
+    uint64_t nodes_visited;    /* BVH nodes visited by extension rays (count=1) */
+    uint64_t tris_tested;      /* triangles tested by extension rays (count=1) */
+    uint64_t shadow_nodes_visited;
+    uint64_t shadow_tris_tested;
+    double kernel_ms_trace;    /* summed kernel time, closest-hit traversal + material sort */
+    double kernel_ms_shadow;   /* summed kernel time, shadow traversal */
+    double kernel_ms_shade;    /* summed kernel time, shading + NEE */
+    double kernel_ms_other;    /* ray generation, film, counters */
+    double wall_ms;            /* host wall time of the call */
+} nr_stats;
+
+/* Copies the message of the last failed call on this thread into buf. */
+int nr_last_error(char* buf, size_t len);
+
+/* Builds a scene from flat arrays: copies it, builds the reference SAH BVH
+ * on the host, uploads triangles, BVH, materials, textures and the emitter
+ * table to the current CUDA device. */
+int nr_scene_create(const nr_scene_desc* desc, nr_scene** out);
+
+/* Builds a scene from the reference's scene-description text: one OBJ path
+ * per line with optional -p x y z, -s k, and forced materials
+ * -m=light r g b | -m=ggx r g b alpha ior | -m=ggxr r g b alpha |
+ * -m=glass r g b ior (src/scene/loader.cpp:26-108). */
+int nr_scene_load(const char* scene_desc, nr_scene** out);
+
+int nr_scene_destroy(nr_scene* scene);
+
+/* info[0..5] = triangles, materials, BVH nodes, BVH depth, emitters, device bytes. */
+int nr_scene_info(const nr_scene* scene, int64_t info[6]);
+
+/* Reads back the flattened scene in loader order (pos 9, uv 6, nrm 9 floats
+ * and a material index per triangle; materials) for checks. Any pointer may
+ * be NULL. */
+int nr_scene_export(const nr_scene* scene, float* pos, float* uv, float* nrm, int32_t* mat, nr_material* mats);
+
+/* BVH in depth-first order (left child first): box[6] per node (min, max),
+ * kids[2] (-1, -1 for a leaf), leaf_first/leaf_count into leaf_tris
+ * (triangle indices in loader order). Returns NR_OK and writes the node count
+ * and leaf-triangle count into *num_nodes / *num_leaf_tris; buffers may be
+ * NULL to query sizes. */
+int nr_bvh_export(const nr_scene* scene, float* box, int32_t* kids, int32_t* leaf_first, int32_t* leaf_count,
+                  int32_t* leaf_tris, int32_t* num_nodes, int32_t* num_leaf_tris);
+
+#define NR_PTR_DEVICE 1  /* flag: the ray and hit arrays are device pointers */
+
+/* Closest hit for n rays (o, d: 3 floats each). tri receives the triangle
+ * index in loader order or -1 for a miss (t = 1e18, b1 = b2 = 0), as
+ * BVH::intersection does. */
+int nr_intersect(nr_scene* scene, int32_t n, const float* o, const float* d, int32_t* tri, float* t, float* b1,
+                 float* b2, int32_t flags);
+
+/* Camera from the reference parameter keys campos, cameuler, camfov, camasp
+ * (defaults 0,0,0 / 0,0,0 / 90 / 1). */
+int nr_camera_from_params(const char* params, nr_camera* cam);
+
+/* Renders the image. params uses the reference grammar ("key=value ..."):
+ * imgw imgh spp prr mis (reference keys and defaults) plus seed (Philox seed,
+ * default 0), rrdepth (first vertex where Russian roulette applies, default 0
+ * as in the reference), maxdepth (0 = unbounded as in the reference),
+ * wave (paths per wavefront batch, default 2^21), sample0 (index of the first
+ * sample, default 0: renders of disjoint sample ranges are independent and
+ * their films sum), profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
+ * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
+ * (W*H*3 bytes: mean^(1/2.2)*255 clamped and truncated, as
+ * src/renderer/rendererptls.cpp:175-180) may each be NULL. cancel, if not
+ * NULL, is polled between waves; 0 cancels (the reference's con_flag).
+ * progress, if not NULL, is called with the percentage done. */
+int nr_render(nr_scene* scene, const nr_camera* cam, const char* params, float* hdr_rgb, uint8_t* rgb8,
+              volatile int32_t* cancel, void (*progress)(float pct, void* user), void* user);
+
+/* Per-sample radiance (after the per-sample max(0, .)) for npix listed pixels
+ * (pix_xy: x, y pairs) and samples [sample0, sample0 + spp): out receives
+ * npix * spp * 3 floats, sample-major within each pixel. Same parameters as
+ * nr_render. */
+int nr_render_samples(nr_scene* scene, const nr_camera* cam, const char* params, int32_t npix,
+                      const int32_t* pix_xy, int32_t sample0, int32_t spp, float* out);
+
+int nr_get_stats(const nr_scene* scene, nr_stats* stats);
+
+/* The CUDA stream (cudaStream_t) on which the scene's kernels run, for
+ * callers that time or order work against it. */
+int nr_scene_stream(const nr_scene* scene, void** stream);
+
+/* Material::bxdf, ::pdf and ::sampleBxdf of scene material `mat` evaluated
+ * on the device for n queries: wo, nrm, wi, uv (3 floats each) and 4
+ * uniforms per query for sampling. Writes f (3), pdf (1), wi_s (3). */
+int nr_material_probe(nr_scene* scene, int32_t mat, int32_t n, const float* wo, const float* nrm, const float* wi,
+                      const float* uv, const float* u, float* f, float* pdf, float* wi_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NURAY_H */

@@ -1,0 +1,645 @@
+// extern "C" boundary of libnuray_gpu.so (include/nuray.h): scene upload
+// and the host loop of the ptnee wavefront.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/nuray.h"
+#include "host_scene.h"
+#include "integrator.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct NrError : std::runtime_error {
+    int code;
+    NrError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define NR_CUDA(call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) {                                                                      \
+            throw NrError(e_ == cudaErrorMemoryAllocation ? NR_ERR_OOM : NR_ERR_CUDA,                 \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+        }                                                                                             \
+    } while (0)
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return NR_OK;
+    } catch (const NrError& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return NR_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return NR_ERR_INVALID;
+    }
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void alloc(size_t n) {
+        release();
+        if (n == 0) return;
+        NR_CUDA(cudaMalloc(&p, n));
+        bytes = n;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct nr_scene {
+    std::mutex mu;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    nr::HostScene host;
+    nr::Bvh bvh;
+    nr::DeviceScene dev{};
+    DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf;
+    int num_gpu_nodes = 0;
+    // wavefront state
+    DevBuf path_mem, film, out_hdr, out_rgb8, pix_list, scratch;
+    nr::PathState ps{};
+    int capacity = 0;
+    uint32_t* counters_host = nullptr;  // pinned
+    nr_stats stats{};
+    std::vector<cudaEvent_t> ev_pool;  // profile=1: events around every kernel group
+
+    ~nr_scene() {
+        if (device >= 0) cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &path_mem, &film,
+                        &out_hdr, &out_rgb8, &pix_list, &scratch})
+            b->release();
+        if (counters_host) cudaFreeHost(counters_host);
+        for (auto& e : ev_pool) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+uint64_t device_bytes(const nr_scene* s) {
+    uint64_t b = 0;
+    for (auto* x : {&s->nodes, &s->tri_geo, &s->tri_shade, &s->mats, &s->texels, &s->tex_info, &s->lights, &s->light_cdf})
+        b += x->bytes;
+    return b;
+}
+
+template <class T>
+void upload(DevBuf& buf, const std::vector<T>& v, cudaStream_t st) {
+    buf.alloc(v.size() * sizeof(T));
+    if (!v.empty()) NR_CUDA(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+inline float bits_f(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
+
+// Flattens triangles in leaf order, converts the BVH into the two-box node
+// layout and builds the emitter table (LightSampler::setPrimitives,
+// src/sampler/lightsampler.cpp:4-39), then copies all of it to the device.
+void upload_scene(nr_scene* s) {
+    const nr::HostScene& H = s->host;
+    const nr::Bvh& B = s->bvh;
+    const int n = H.num_tris();
+    cudaStream_t st = s->stream;
+
+    std::vector<float4> geo(3 * (size_t)n), shade(4 * (size_t)n);
+    for (int k = 0; k < n; ++k) {
+        int i = B.leaf_tris[k];
+        const float* p = &H.pos[9 * (size_t)i];
+        const float* t = &H.uv[6 * (size_t)i];
+        const float* nn = &H.nrm[9 * (size_t)i];
+        geo[3 * k] = make_float4(p[0], p[1], p[2], bits_f(i));
+        geo[3 * k + 1] = make_float4(p[3] - p[0], p[4] - p[1], p[5] - p[2], bits_f(H.mat[i]));
+        geo[3 * k + 2] = make_float4(p[6] - p[0], p[7] - p[1], p[8] - p[2], 0.0f);
+        shade[4 * k] = make_float4(nn[0], nn[1], nn[2], t[0]);
+        shade[4 * k + 1] = make_float4(nn[3], nn[4], nn[5], t[1]);
+        shade[4 * k + 2] = make_float4(nn[6], nn[7], nn[8], t[2]);
+        shade[4 * k + 3] = make_float4(t[3], t[4], t[5], bits_f(H.mat[i]));
+    }
+
+    // internal nodes get consecutive GPU indices in depth-first order
+    std::vector<int> gpu_index(B.nodes.size(), -1);
+    int ng = 0;
+    for (size_t i = 0; i < B.nodes.size(); ++i)
+        if (B.nodes[i].left >= 0) gpu_index[i] = ng++;
+    auto ref_of = [&](int i) {
+        const nr::BvhNode& c = B.nodes[i];
+        return c.left >= 0 ? gpu_index[i] : nr::leaf_ref(c.first, c.count);
+    };
+    std::vector<nr::GpuNode> gn(ng);
+    for (size_t i = 0; i < B.nodes.size(); ++i) {
+        const nr::BvhNode& N = B.nodes[i];
+        if (N.left < 0) continue;
+        const nr::BvhNode& L = B.nodes[N.left];
+        const nr::BvhNode& R = B.nodes[N.right];
+        nr::GpuNode& g = gn[gpu_index[i]];
+        g.a = make_float4(L.lo[0], L.hi[0], L.lo[1], L.hi[1]);
+        g.b = make_float4(R.lo[0], R.hi[0], R.lo[1], R.hi[1]);
+        g.c = make_float4(L.lo[2], L.hi[2], R.lo[2], R.hi[2]);
+        g.d = make_int4(ref_of(N.left), ref_of(N.right), N.depth, 0);
+    }
+    s->num_gpu_nodes = ng;
+
+    // emitters in loader order, weight = Triangle::area (twice the area)
+    std::vector<float4> lt;
+    std::vector<float> pdf;
+    float sum = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        const nr_material& M = H.mats[H.mat[i]];
+        if (M.type != NR_MAT_LIGHT) continue;
+        const float* p = &H.pos[9 * (size_t)i];
+        const float* nn = &H.nrm[9 * (size_t)i];
+        float e1[3] = {p[3] - p[0], p[4] - p[1], p[5] - p[2]};
+        float e2[3] = {p[6] - p[0], p[7] - p[1], p[8] - p[2]};
+        float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        float w = (float)std::sqrt((double)(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+        pdf.push_back(w);
+        sum += w;
+        lt.push_back(make_float4(p[0], p[1], p[2], M.c0[0]));
+        lt.push_back(make_float4(p[3], p[4], p[5], M.c0[1]));
+        lt.push_back(make_float4(p[6], p[7], p[8], M.c0[2]));
+        lt.push_back(make_float4(nn[0], nn[1], nn[2], 0.0f));
+        lt.push_back(make_float4(nn[3], nn[4], nn[5], 0.0f));
+        lt.push_back(make_float4(nn[6], nn[7], nn[8], 0.0f));
+    }
+    sum = (float)((double)sum + 1e-8);
+    std::vector<float> cdf;
+    float acc = 1e-6f;
+    for (float& x : pdf) { x /= sum; acc += x; cdf.push_back(acc); }
+
+    std::vector<float4> texels;
+    std::vector<int4> tinfo;
+    size_t off = 0;
+    for (size_t t = 0; t < H.tex_wh.size() / 2; ++t) {
+        int w = H.tex_wh[2 * t], h = H.tex_wh[2 * t + 1];
+        tinfo.push_back(make_int4(w, h, (int)(off / 1), 0));
+        for (size_t k = 0; k < (size_t)w * h; ++k) {
+            const float* c = &H.tex_data[3 * (off + k)];
+            texels.push_back(make_float4(c[0], c[1], c[2], 0.0f));
+        }
+        off += (size_t)w * h;
+    }
+    if (off > (size_t)INT32_MAX) throw NrError(NR_ERR_INVALID, "textures exceed 2^31 texels");
+
+    upload(s->tri_geo, geo, st);
+    upload(s->tri_shade, shade, st);
+    upload(s->nodes, gn, st);
+    upload(s->mats, H.mats, st);
+    upload(s->texels, texels, st);
+    upload(s->tex_info, tinfo, st);
+    upload(s->lights, lt, st);
+    upload(s->light_cdf, cdf, st);
+    NR_CUDA(cudaStreamSynchronize(st));
+
+    nr::DeviceScene& D = s->dev;
+    D.nodes = s->nodes.as<nr::GpuNode>();
+    D.tri_geo = s->tri_geo.as<float4>();
+    D.tri_shade = s->tri_shade.as<float4>();
+    D.mats = s->mats.as<nr_material>();
+    D.tex_texels = s->texels.as<float4>();
+    D.tex_info = s->tex_info.as<int4>();
+    D.lights = s->lights.as<float4>();
+    D.light_cdf = s->light_cdf.as<float>();
+    D.num_lights = (int)pdf.size();
+    D.light_p = (float)(1.0 / ((double)sum + 1e-8));
+    D.num_tris = n;
+    D.num_mats = (int)H.mats.size();
+    D.env_tex = H.env_tex;
+    D.env_gain = H.env_gain;
+    D.max_depth = B.max_depth;
+    if (n == 0) {
+        D.root_ref = INT32_MIN;
+    } else {
+        const nr::BvhNode& R = B.nodes[0];
+        D.root_ref = R.left >= 0 ? 0 : nr::leaf_ref(R.first, R.count);
+        for (int k = 0; k < 3; ++k) { D.root_lo[k] = R.lo[k]; D.root_hi[k] = R.hi[k]; }
+    }
+}
+
+void finish_scene(nr_scene* s) {
+    NR_CUDA(cudaGetDevice(&s->device));
+    NR_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device));
+    NR_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    NR_CUDA(cudaMallocHost(&s->counters_host, nr::NUM_COUNTERS * sizeof(uint32_t)));
+    int threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    nr::build_bvh(s->host, s->bvh, threads);
+    if (s->bvh.max_depth + 2 > NR_STACK_LIMIT)
+        throw NrError(NR_ERR_INVALID, "BVH depth " + std::to_string(s->bvh.max_depth) + " exceeds the traversal stack");
+    nr::launch_setup(s->num_sms);
+    upload_scene(s);
+}
+
+// Sizes the path-state buffers for `cap` slots.
+void ensure_paths(nr_scene* s, int cap) {
+    if (cap <= s->capacity) return;
+    const size_t C = (size_t)cap;
+    const size_t f4 = 16;
+    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 2 + C * 4 * nr::NUM_CAT + C * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
+    s->path_mem.alloc(bytes);
+    char* p = s->path_mem.as<char>();
+    auto take = [&](size_t n) { char* r = p; p += (n + 255) & ~size_t(255); return r; };
+    nr::PathState& P = s->ps;
+    P.ray_o = (float4*)take(C * f4);
+    P.ray_d = (float4*)take(C * f4);
+    P.hit = (float4*)take(C * f4);
+    P.thr = (float4*)take(C * f4);
+    P.rad = (float4*)take(C * f4);
+    P.meta = (uint4*)take(C * 16);
+    P.queue_in = (int32_t*)take(C * 4);
+    P.queue_out = (int32_t*)take(C * 4);
+    P.sorted = (int32_t*)take(C * 4 * nr::NUM_CAT);
+    P.sh_o = (float4*)take(C * f4);
+    P.sh_d = (float4*)take(C * f4);
+    P.sh_c = (float4*)take(C * f4);
+    P.counters = (uint32_t*)take(nr::NUM_COUNTERS * 4);
+    NR_CUDA(cudaMemsetAsync(P.counters, 0, nr::NUM_COUNTERS * 4, s->stream));
+    s->capacity = cap;
+}
+
+struct RenderArgs {
+    nr::Policy pol;
+    nr_camera cam;
+    int spp;
+    int wave;
+    bool profile;
+    bool count;
+    int sample0;
+};
+
+RenderArgs parse_args(const nr_camera* cam, const char* params) {
+    nr::Config c(params);
+    RenderArgs a;
+    a.pol.prr = c.get_float("prr", 0.8f);
+    a.pol.mis = c.get_int("mis", 1) != 0 ? 1 : 0;
+    a.pol.rrdepth = c.get_int("rrdepth", 0);
+    a.pol.maxdepth = c.get_int("maxdepth", 0);
+    uint64_t seed = 0;
+    std::string ss = c.get_str("seed");
+    if (!ss.empty()) seed = std::stoull(ss);
+    a.pol.seed_lo = (uint32_t)seed;
+    a.pol.seed_hi = (uint32_t)(seed >> 32);
+    a.pol.imgw = c.get_int("imgw", 1);
+    a.pol.imgh = c.get_int("imgh", 1);
+    a.spp = c.get_int("spp", 1);
+    a.wave = c.get_int("wave", 1 << 21);
+    a.profile = c.get_int("profile", 0) != 0;
+    a.count = c.get_int("count", 0) != 0;
+    a.sample0 = c.get_int("sample0", 0);
+    if (a.sample0 < 0) throw NrError(NR_ERR_INVALID, "sample0 must be >= 0");
+    if (a.pol.imgw <= 0 || a.pol.imgh <= 0) throw NrError(NR_ERR_INVALID, "imgw and imgh must be positive");
+    if ((int64_t)a.pol.imgw * a.pol.imgh > (1LL << 30)) throw NrError(NR_ERR_INVALID, "image too large");
+    if (a.spp <= 0) throw NrError(NR_ERR_INVALID, "spp must be positive");
+    if (a.wave <= 0) throw NrError(NR_ERR_INVALID, "wave must be positive");
+    if (a.pol.maxdepth < 0 || a.pol.rrdepth < 0) throw NrError(NR_ERR_INVALID, "rrdepth and maxdepth must be >= 0");
+    a.cam = cam ? *cam : nr::camera_from_config(c);
+    return a;
+}
+
+// Traces all paths of [0, npix * spp) in waves. Per wave: ray generation,
+// then trace/shade/shadow bounces until no path is live, then either the
+// film accumulation (film != null) or the per-sample copy (out != null).
+void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pix, int sample0, float4* film,
+               float* dev_out, volatile int32_t* cancel, void (*progress)(float, void*), void* user) {
+    const uint64_t total = (uint64_t)npix * (uint64_t)A.spp;
+    const int cap = (int)std::min<uint64_t>(total, (uint64_t)A.wave);
+    ensure_paths(s, cap);
+    cudaStream_t st = s->stream;
+    const float film_h = nr::film_height(A.cam);
+    auto t0 = std::chrono::steady_clock::now();
+    nr_stats& S = s->stats;
+    S = nr_stats{};
+    // profile=1: events are recorded in sequence and read once at the end,
+    // so the host never waits on them inside the loop.
+    size_t nev = 0;
+    std::vector<int> ev_kind;  // kernel group that ends at event i (0 trace, 1 shade, 2 shadow, 3 other)
+    auto mark = [&](int kind) {
+        if (!A.profile) return;
+        if (nev == s->ev_pool.size()) {
+            cudaEvent_t e;
+            NR_CUDA(cudaEventCreate(&e));
+            s->ev_pool.push_back(e);
+        }
+        NR_CUDA(cudaEventRecord(s->ev_pool[nev++], st));
+        ev_kind.push_back(kind);
+    };
+    NR_CUDA(cudaMemsetAsync(s->ps.counters, 0, nr::NUM_COUNTERS * 4, st));
+    S.kernel_launches = 0;
+    for (uint64_t base = 0; base < total; base += (uint64_t)cap) {
+        if (cancel && *cancel == 0) throw NrError(NR_ERR_CANCELLED, "cancelled");
+        nr::WaveDesc W;
+        W.base = base;
+        W.count = (int)std::min<uint64_t>((uint64_t)cap, total - base);
+        W.npix = npix;
+        W.sample0 = (uint32_t)sample0;
+        W.pix_xy = dev_pix;
+        mark(-1);
+        nr::launch_reset_counters(s->ps.counters, st);
+        nr::launch_raygen(s->ps, W, A.cam, film_h, A.pol, st);
+        S.kernel_launches += 2;
+        mark(3);
+        int live = W.count;
+        for (int bounce = 0;; ++bounce) {
+            if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
+            cudaEvent_t evs[4];
+            if (A.profile) {
+                while (s->ev_pool.size() < nev + 4) {
+                    cudaEvent_t e;
+                    NR_CUDA(cudaEventCreate(&e));
+                    s->ev_pool.push_back(e);
+                }
+                for (int k = 0; k < 4; ++k) evs[k] = s->ev_pool[nev + k];
+                ev_kind.push_back(-1); ev_kind.push_back(0); ev_kind.push_back(1); ev_kind.push_back(2);
+                nev += 4;
+            }
+            nr::launch_bounce(s->ps, s->dev, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count);
+            S.bounces++;
+            S.trace_launches++;
+            S.kernel_launches += 4;
+            // With a depth limit the loop runs exactly maxdepth bounces; without
+            // one the live count is read back to find the end of the wave.
+            if (A.pol.maxdepth == 0 || bounce >= 4) {
+                NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters, nr::NUM_COUNTERS * 4, cudaMemcpyDeviceToHost, st));
+                NR_CUDA(cudaStreamSynchronize(st));
+                live = (int)s->counters_host[nr::CNT_IN];
+                if (live == 0) break;
+            }
+        }
+        mark(-1);
+        if (film) nr::launch_film(s->ps, W, film, st);
+        if (dev_out) nr::launch_collect(s->ps, W, dev_out, A.spp, st);
+        S.kernel_launches += 1;
+        mark(3);
+        S.waves++;
+        if (progress) {
+            NR_CUDA(cudaStreamSynchronize(st));
+            progress((float)(100.0 * (double)(base + W.count) / (double)total), user);
+        }
+    }
+    NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters, nr::NUM_COUNTERS * 4, cudaMemcpyDeviceToHost, st));
+    NR_CUDA(cudaStreamSynchronize(st));
+    NR_CUDA(cudaGetLastError());
+    uint32_t* c = s->counters_host;
+    auto u64 = [&](int i) { return (uint64_t)c[i] | ((uint64_t)c[i + 1] << 32); };
+    S.paths = total;
+    S.rays = u64(nr::CNT_RAYS);
+    S.shadow_rays = u64(nr::CNT_SHRAYS);
+    S.nodes_visited = u64(nr::CNT_NODES);
+    S.tris_tested = u64(nr::CNT_TRIS);
+    S.shadow_nodes_visited = u64(nr::CNT_SH_NODES);
+    S.shadow_tris_tested = u64(nr::CNT_SH_TRIS);
+    for (size_t i = 1; i < nev; ++i) {
+        if (ev_kind[i] < 0) continue;
+        float ms = 0.0f;
+        NR_CUDA(cudaEventElapsedTime(&ms, s->ev_pool[i - 1], s->ev_pool[i]));
+        double* dst[4] = {&S.kernel_ms_trace, &S.kernel_ms_shade, &S.kernel_ms_shadow, &S.kernel_ms_other};
+        *dst[ev_kind[i]] += ms;
+    }
+    S.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (c[nr::CNT_ERR] != 0) throw NrError(NR_ERR_DEVICE, "traversal stack overflow in a kernel");
+}
+
+}  // namespace
+
+extern "C" {
+
+int nr_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return NR_ERR_INVALID;
+    std::strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+    return NR_OK;
+}
+
+int nr_scene_create(const nr_scene_desc* desc, nr_scene** out) {
+    return guarded([&]() {
+        if (!desc || !out) throw NrError(NR_ERR_INVALID, "null argument");
+        *out = nullptr;
+        auto s = std::make_unique<nr_scene>();
+        std::string err = nr::scene_from_desc(*desc, s->host);
+        if (!err.empty()) throw NrError(NR_ERR_INVALID, err);
+        finish_scene(s.get());
+        *out = s.release();
+    });
+}
+
+int nr_scene_load(const char* text, nr_scene** out) {
+    return guarded([&]() {
+        if (!text || !out) throw NrError(NR_ERR_INVALID, "null argument");
+        *out = nullptr;
+        auto s = std::make_unique<nr_scene>();
+        std::string err = nr::scene_from_text(text, s->host);
+        if (!err.empty()) throw NrError(err.rfind("cannot open", 0) == 0 ? NR_ERR_IO : NR_ERR_INVALID, err);
+        finish_scene(s.get());
+        *out = s.release();
+    });
+}
+
+int nr_scene_destroy(nr_scene* s) {
+    return guarded([&]() { delete s; });
+}
+
+int nr_scene_info(const nr_scene* s, int64_t info[6]) {
+    return guarded([&]() {
+        if (!s || !info) throw NrError(NR_ERR_INVALID, "null argument");
+        info[0] = s->host.num_tris();
+        info[1] = (int64_t)s->host.mats.size();
+        info[2] = (int64_t)s->bvh.nodes.size();
+        info[3] = s->bvh.max_depth;
+        info[4] = s->dev.num_lights;
+        info[5] = (int64_t)device_bytes(s);
+    });
+}
+
+int nr_scene_export(const nr_scene* s, float* pos, float* uv, float* nrm, int32_t* mat, nr_material* mats) {
+    return guarded([&]() {
+        if (!s) throw NrError(NR_ERR_INVALID, "null scene");
+        const nr::HostScene& H = s->host;
+        if (pos) std::copy(H.pos.begin(), H.pos.end(), pos);
+        if (uv) std::copy(H.uv.begin(), H.uv.end(), uv);
+        if (nrm) std::copy(H.nrm.begin(), H.nrm.end(), nrm);
+        if (mat) std::copy(H.mat.begin(), H.mat.end(), mat);
+        if (mats) std::copy(H.mats.begin(), H.mats.end(), mats);
+    });
+}
+
+int nr_bvh_export(const nr_scene* s, float* box, int32_t* kids, int32_t* leaf_first, int32_t* leaf_count,
+                  int32_t* leaf_tris, int32_t* num_nodes, int32_t* num_leaf_tris) {
+    return guarded([&]() {
+        if (!s) throw NrError(NR_ERR_INVALID, "null scene");
+        const nr::Bvh& B = s->bvh;
+        for (size_t i = 0; i < B.nodes.size(); ++i) {
+            const nr::BvhNode& n = B.nodes[i];
+            if (box) for (int k = 0; k < 3; ++k) { box[6 * i + k] = n.lo[k]; box[6 * i + 3 + k] = n.hi[k]; }
+            if (kids) { kids[2 * i] = n.left; kids[2 * i + 1] = n.right; }
+            if (leaf_first) leaf_first[i] = n.first;
+            if (leaf_count) leaf_count[i] = n.count;
+        }
+        if (leaf_tris) std::copy(B.leaf_tris.begin(), B.leaf_tris.end(), leaf_tris);
+        if (num_nodes) *num_nodes = (int32_t)B.nodes.size();
+        if (num_leaf_tris) *num_leaf_tris = (int32_t)B.leaf_tris.size();
+    });
+}
+
+int nr_intersect(nr_scene* s, int32_t n, const float* o, const float* d, int32_t* tri, float* t, float* b1, float* b2,
+                 int32_t flags) {
+    return guarded([&]() {
+        if (!s || n < 0 || (n > 0 && (!o || !d || !tri || !t || !b1 || !b2))) throw NrError(NR_ERR_INVALID, "bad argument");
+        if (n == 0) return;
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        ensure_paths(s, 1);
+        cudaStream_t st = s->stream;
+        const float *dO = o, *dD = d;
+        int32_t* dTri = tri;
+        float *dT = t, *dB1 = b1, *dB2 = b2;
+        if (!(flags & NR_PTR_DEVICE)) {
+            size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4;
+            s->scratch.alloc(2 * f3 + 4 * f1 + 4 * 256);
+            char* p = s->scratch.as<char>();
+            auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
+            float* xo = (float*)take(f3);
+            float* xd = (float*)take(f3);
+            dTri = (int32_t*)take(f1); dT = (float*)take(f1); dB1 = (float*)take(f1); dB2 = (float*)take(f1);
+            NR_CUDA(cudaMemcpyAsync(xo, o, f3, cudaMemcpyHostToDevice, st));
+            NR_CUDA(cudaMemcpyAsync(xd, d, f3, cudaMemcpyHostToDevice, st));
+            dO = xo; dD = xd;
+        }
+        NR_CUDA(cudaMemsetAsync(s->ps.counters + nr::CNT_ERR, 0, 4, st));
+        nr::launch_intersect(s->dev, n, dO, dD, dTri, dT, dB1, dB2, s->ps.counters + nr::CNT_ERR, st);
+        NR_CUDA(cudaGetLastError());
+        if (!(flags & NR_PTR_DEVICE)) {
+            size_t f1 = (size_t)n * 4;
+            NR_CUDA(cudaMemcpyAsync(tri, dTri, f1, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaMemcpyAsync(t, dT, f1, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaMemcpyAsync(b1, dB1, f1, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaMemcpyAsync(b2, dB2, f1, cudaMemcpyDeviceToHost, st));
+        }
+        uint32_t err = 0;
+        NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters + nr::CNT_ERR, 4, cudaMemcpyDeviceToHost, st));
+        NR_CUDA(cudaStreamSynchronize(st));
+        err = s->counters_host[0];
+        if (err) throw NrError(NR_ERR_DEVICE, "traversal stack overflow in a kernel");
+    });
+}
+
+int nr_camera_from_params(const char* params, nr_camera* cam) {
+    return guarded([&]() {
+        if (!cam) throw NrError(NR_ERR_INVALID, "null camera");
+        *cam = nr::camera_from_config(nr::Config(params));
+    });
+}
+
+int nr_render(nr_scene* s, const nr_camera* cam, const char* params, float* hdr_rgb, uint8_t* rgb8,
+              volatile int32_t* cancel, void (*progress)(float, void*), void* user) {
+    return guarded([&]() {
+        if (!s) throw NrError(NR_ERR_INVALID, "null scene");
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        RenderArgs A = parse_args(cam, params);
+        const int npix = A.pol.imgw * A.pol.imgh;
+        cudaStream_t st = s->stream;
+        s->film.alloc((size_t)npix * sizeof(float4));
+        NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
+        run_waves(s, A, npix, nullptr, A.sample0, s->film.as<float4>(), nullptr, cancel, progress, user);
+        if (hdr_rgb || rgb8) {
+            if (hdr_rgb && s->out_hdr.bytes < (size_t)npix * 12) s->out_hdr.alloc((size_t)npix * 12);
+            if (rgb8 && s->out_rgb8.bytes < (size_t)npix * 3) s->out_rgb8.alloc((size_t)npix * 3);
+            nr::launch_finish(s->film.as<float4>(), npix, 1.0f / (float)A.spp, hdr_rgb ? s->out_hdr.as<float>() : nullptr,
+                              rgb8 ? s->out_rgb8.as<uint8_t>() : nullptr, st);
+            if (hdr_rgb) NR_CUDA(cudaMemcpyAsync(hdr_rgb, s->out_hdr.p, (size_t)npix * 12, cudaMemcpyDeviceToHost, st));
+            if (rgb8) NR_CUDA(cudaMemcpyAsync(rgb8, s->out_rgb8.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+        }
+        NR_CUDA(cudaGetLastError());
+    });
+}
+
+int nr_render_samples(nr_scene* s, const nr_camera* cam, const char* params, int32_t npix, const int32_t* pix_xy,
+                      int32_t sample0, int32_t spp, float* out) {
+    return guarded([&]() {
+        if (!s || npix <= 0 || !pix_xy || spp <= 0 || !out || sample0 < 0) throw NrError(NR_ERR_INVALID, "bad argument");
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        RenderArgs A = parse_args(cam, params);
+        A.spp = spp;
+        for (int32_t i = 0; i < npix; ++i)
+            if (pix_xy[2 * i] < 0 || pix_xy[2 * i] >= A.pol.imgw || pix_xy[2 * i + 1] < 0 || pix_xy[2 * i + 1] >= A.pol.imgh)
+                throw NrError(NR_ERR_INVALID, "pixel outside the image");
+        cudaStream_t st = s->stream;
+        size_t nout = (size_t)npix * spp * 3;
+        s->pix_list.alloc((size_t)npix * 8);
+        s->out_hdr.alloc(nout * 4);
+        NR_CUDA(cudaMemcpyAsync(s->pix_list.p, pix_xy, (size_t)npix * 8, cudaMemcpyHostToDevice, st));
+        run_waves(s, A, npix, s->pix_list.as<int32_t>(), sample0, nullptr, s->out_hdr.as<float>(), nullptr, nullptr, nullptr);
+        NR_CUDA(cudaMemcpyAsync(out, s->out_hdr.p, nout * 4, cudaMemcpyDeviceToHost, st));
+        NR_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int nr_get_stats(const nr_scene* s, nr_stats* st) {
+    return guarded([&]() {
+        if (!s || !st) throw NrError(NR_ERR_INVALID, "null argument");
+        *st = s->stats;
+    });
+}
+
+int nr_scene_stream(const nr_scene* s, void** stream) {
+    return guarded([&]() {
+        if (!s || !stream) throw NrError(NR_ERR_INVALID, "null argument");
+        *stream = (void*)s->stream;
+    });
+}
+
+int nr_material_probe(nr_scene* s, int32_t mat, int32_t n, const float* wo, const float* nrm, const float* wi,
+                      const float* uv, const float* u, float* f, float* pdf, float* wi_s) {
+    return guarded([&]() {
+        if (!s || n < 0 || mat < 0 || mat >= (int)s->host.mats.size()) throw NrError(NR_ERR_INVALID, "bad argument");
+        if (n == 0) return;
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        cudaStream_t st = s->stream;
+        size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4, f4 = (size_t)n * 16;
+        s->scratch.alloc(4 * f3 + f4 + 2 * f3 + f1 + 16 * 256);
+        char* p = s->scratch.as<char>();
+        auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
+        float *dwo = (float*)take(f3), *dn = (float*)take(f3), *dwi = (float*)take(f3), *duv = (float*)take(f3);
+        float *du = (float*)take(f4), *df = (float*)take(f3), *dws = (float*)take(f3), *dp = (float*)take(f1);
+        NR_CUDA(cudaMemcpyAsync(dwo, wo, f3, cudaMemcpyHostToDevice, st));
+        NR_CUDA(cudaMemcpyAsync(dn, nrm, f3, cudaMemcpyHostToDevice, st));
+        NR_CUDA(cudaMemcpyAsync(dwi, wi, f3, cudaMemcpyHostToDevice, st));
+        NR_CUDA(cudaMemcpyAsync(duv, uv, f3, cudaMemcpyHostToDevice, st));
+        NR_CUDA(cudaMemcpyAsync(du, u, f4, cudaMemcpyHostToDevice, st));
+        nr::launch_material_probe(s->dev, mat, n, dwo, dn, dwi, duv, du, df, dp, dws, st);
+        NR_CUDA(cudaGetLastError());
+        NR_CUDA(cudaMemcpyAsync(f, df, f3, cudaMemcpyDeviceToHost, st));
+        NR_CUDA(cudaMemcpyAsync(pdf, dp, f1, cudaMemcpyDeviceToHost, st));
+        NR_CUDA(cudaMemcpyAsync(wi_s, dws, f3, cudaMemcpyDeviceToHost, st));
+        NR_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Host side of libnuray_gpu.so: the reference's parameter grammar, scene
+// loading and flattening, and the SAH BVH build.
+#pragma once
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/nuray.h"
+
+namespace nr {
+
+// Config (src/utils/config.cpp): whitespace-separated key=value items split
+// at the first '='; typed getters return the default when the key is absent
+// or does not parse; vec3 values are comma-separated.
+class Config {
+public:
+    explicit Config(const char* text = nullptr);
+    void add_item(const std::string& kv);
+    bool has(const std::string& key) const { return mp_.count(key) != 0; }
+    std::string get_str(const std::string& key) const;  // "" when absent, as the reference
+    int get_int(const std::string& key, int def) const;
+    float get_float(const std::string& key, float def) const;
+    bool get_vec3(const std::string& key, float out[3]) const;
+
+private:
+    std::map<std::string, std::string> mp_;
+};
+
+// Camera as Cmd::main builds it (src/cmd/cmd.cpp:99-101, src/scene/camera.cpp:88-105).
+nr_camera camera_from_config(const Config& c);
+// 2 tan(fov * 3.14159 / 180 / 2) evaluated in double as the reference, to float.
+float film_height(const nr_camera& cam);
+
+// Flattened scene in loader order.
+struct HostScene {
+    std::vector<float> pos;   // 9 per triangle
+    std::vector<float> uv;    // 6 per triangle
+    std::vector<float> nrm;   // 9 per triangle
+    std::vector<int32_t> mat;
+    std::vector<nr_material> mats;
+    std::vector<int32_t> tex_wh;
+    std::vector<float> tex_data;
+    int32_t env_tex = -1;
+    float env_gain = 1.0f;
+    int num_tris() const { return (int)mat.size(); }
+};
+
+// Copies a caller description, applying the Triangle constructor's
+// face-normal rule (src/scene/triangle.cpp:12-25). Returns "" or an error.
+std::string scene_from_desc(const nr_scene_desc& d, HostScene& out);
+
+// Loader::fromSceneDescription / loadObj / loadMtl (src/scene/loader.cpp).
+// Texture maps referenced by MTL files must be PFM or binary PPM files
+// (the reference decodes PNG/JPG through Qt, which this library does not
+// link). Returns "" or an error message.
+std::string scene_from_text(const std::string& desc, HostScene& out);
+
+// Reads a PFM (float) or binary PPM (8-bit, decoded with c^2.2 as
+// Texture::load does) image into linear RGB floats.
+std::string read_image(const std::string& path, int& w, int& h, std::vector<float>& rgb);
+
+// Binary BVH with the reference's SAH (BVH::_divide, src/hierarchy/bvh.cpp:5-58):
+// primitives sorted by pMax along each axis, prefix/suffix surface-area sweep
+// with cost SA_L * |L| + SA_R * (|R| + 1), leaves of at most 5 triangles.
+// Nodes are stored depth-first, left child first.
+struct BvhNode {
+    float lo[3], hi[3];
+    int32_t left, right;      // -1 for a leaf
+    int32_t first, count;     // into leaf_tris for a leaf
+    int32_t depth;
+};
+struct Bvh {
+    std::vector<BvhNode> nodes;
+    std::vector<int32_t> leaf_tris;  // triangle indices (loader order), leaves depth-first
+    int32_t max_depth = 0;
+};
+void build_bvh(const HostScene& s, Bvh& out, int threads);
+
+}  // namespace nr

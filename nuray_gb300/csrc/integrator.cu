@@ -1,0 +1,431 @@
+// The ptnee wavefront: ray generation, closest-hit traversal with the
+// material sort, shading with NEE / MIS / Russian roulette, shadow
+// traversal, film accumulation. One path per (pixel, sample); its random
+// numbers come from a Philox stream keyed by (pixel, sample) so any batch
+// split and any thread order give the same image.
+//
+// Per path and vertex this is RendererPTLS::trace
+// (src/renderer/rendererptls.cpp:13-94) unrolled into an iteration:
+//   L += T * (NEE term);  T *= |wi.n| f / pdf / prr;  emitter hit: L += T * Ke * fac
+// which is the reference's recursion result = NEE + Li * |wi.n| f / pdf / prr.
+#include "nr_material.cuh"
+#include "integrator.h"
+
+namespace nr {
+
+// Warp-aggregated append: every active lane with `want` gets a unique index
+// in the queue behind *counter; one atomic per warp.
+__device__ __forceinline__ int warp_append(bool want, uint32_t* counter) {
+    unsigned active = __activemask();
+    unsigned m = __ballot_sync(active, want);
+    if (!want) return -1;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int rank = __popc(m & ((1u << lane) - 1u));
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return (int)(base + rank);
+}
+
+// Append keyed by a small category: lanes sharing a key share one atomic.
+__device__ __forceinline__ int warp_append_keyed(int key, uint32_t* counters) {
+    unsigned active = __activemask();
+    unsigned m = __match_any_sync(active, key);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int rank = __popc(m & ((1u << lane) - 1u));
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&counters[key], (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return (int)(base + rank);
+}
+
+// ---------------------------------------------------------------- ray generation
+// RendererPTLS::render per-sample body (src/renderer/rendererptls.cpp:170-173):
+// jitter x, jitter y, Camera::generateRay.
+__global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, Policy pol) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W.count) return;
+    uint64_t g = W.base + (uint64_t)i;
+    uint32_t srel = (uint32_t)(g / (uint64_t)W.npix);
+    uint32_t pidx = (uint32_t)(g % (uint64_t)W.npix);
+    int x, y;
+    if (W.pix_xy) { x = W.pix_xy[2 * pidx]; y = W.pix_xy[2 * pidx + 1]; }
+    else { x = (int)(pidx % (uint32_t)pol.imgw); y = (int)(pidx / (uint32_t)pol.imgw); }
+    uint32_t key = (uint32_t)y * (uint32_t)pol.imgw + (uint32_t)x;
+    uint32_t sample = W.sample0 + srel;
+    Stream s;
+    s.init(pol.seed_lo, pol.seed_hi, key, sample, 0);
+    float jx = s.next();
+    float jy = s.next();
+    f3 d = camera_ray(cam, film_h, (float)x + jx, (float)y + jy, (float)pol.imgw, (float)pol.imgh);
+    P.ray_o[i] = make_float4(cam.pos[0], cam.pos[1], cam.pos[2], 0.f);
+    P.ray_d[i] = make_float4(d.x, d.y, d.z, 0.f);
+    P.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+    P.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.meta[i] = make_uint4(key, sample, s.n, 0u);
+    P.queue_in[i] = i;
+    if (i == 0) P.counters[CNT_IN] = (uint32_t)W.count;
+}
+
+// ---------------------------------------------------------------- closest hit + sort
+// Persistent: warps take 32 queue entries at a time from a shared cursor.
+// Writes the hit record and buckets the slot by shading category
+// (material type of the hit, or CAT_MISS) for the shading pass.
+// Adds a per-thread count into a 64-bit device counter, one atomic per warp.
+__device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(reinterpret_cast<unsigned long long*>(lohi), x);
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int capacity) {
+    const uint32_t n = P.counters[CNT_IN];
+    const int lane = threadIdx.x & 31;
+    uint32_t nv = 0, nt = 0;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t idx = base + lane;
+        if (idx < n) {
+            int slot = P.queue_in[idx];
+            f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
+            float t, b1, b2;
+            int tri = closest_hit(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                  COUNT ? &nt : nullptr);
+            P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
+            int cat = CAT_MISS;
+            if (tri >= 0) cat = S.mats[__float_as_int(__ldg(&S.tri_geo[3 * tri + 1]).w)].type;
+            int pos = warp_append_keyed(cat, &P.counters[CNT_CAT]);
+            P.sorted[(size_t)cat * capacity + pos] = slot;
+        }
+    }
+    if (COUNT) {
+        warp_count(nv, &P.counters[CNT_NODES]);
+        warp_count(nt, &P.counters[CNT_TRIS]);
+    }
+}
+
+// ---------------------------------------------------------------- shading
+__device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot) {
+    float4 h = P.hit[slot];
+    float4 thr = P.thr[slot];
+    uint4 meta = P.meta[slot];
+    f3 dir = xyz(P.ray_d[slot]);
+    f3 T = xyz(thr);
+    int tri = __float_as_int(h.w);
+    if (tri < 0) {
+        if (S.env_tex >= 0) {
+            float4 r = P.rad[slot];
+            f3 e = env_lookup(S, dir);
+            P.rad[slot] = make_float4(r.x + T.x * e.x, r.y + T.y * e.y, r.z + T.z * e.z, 0.f);
+        }
+        return;
+    }
+    float b1 = h.y, b2 = h.z;
+    float4 s0 = __ldg(&S.tri_shade[4 * tri]), s1 = __ldg(&S.tri_shade[4 * tri + 1]);
+    float4 s2 = __ldg(&S.tri_shade[4 * tri + 2]), s3 = __ldg(&S.tri_shade[4 * tri + 3]);
+    int mat = __float_as_int(s3.w);
+    // Triangle::getNormal / getTexCoords (src/scene/triangle.cpp:35-43)
+    float w0 = 1.0f - b1 - b2;
+    f3 normal = normalized(w0 * xyz(s0) + b1 * xyz(s1) + b2 * xyz(s2));
+    f3 wo = -dir;
+    const int type = S.mats[mat].type;
+    if (type == NR_MAT_LIGHT) {  // emitter: Ke * light_fac (rendererptls.cpp:33-36)
+        const nr_material& M = S.mats[mat];
+        float4 r = P.rad[slot];
+        float lf = thr.w;
+        P.rad[slot] = make_float4(r.x + T.x * M.c0[0] * lf, r.y + T.y * M.c0[1] * lf, r.z + T.z * M.c0[2] * lf, 0.f);
+        return;
+    }
+    // opaque back faces end the path (rendererptls.cpp:41-42)
+    if (dot(normal, dir) > 0.f && !mat_transmissive(type)) return;
+    // texture coordinates: t0 = (s0.w, s1.w), t1 = (s2.w, s3.x), t2 = (s3.y, s3.z)
+    f3 uv = mk(w0 * s0.w + b1 * s2.w + b2 * s3.y, w0 * s1.w + b1 * s3.x + b2 * s3.z, 0.f);
+    MatView M = load_mat(S, mat, uv);
+    f3 o = xyz(P.ray_o[slot]);
+    f3 hit_pos = o + dir * h.x;
+    Stream rng;
+    rng.init(pol.seed_lo, pol.seed_hi, meta.x, meta.y, meta.z);
+    float fac = 1.0f;
+    const int depth = (int)meta.w;
+
+    // next-event estimation (rendererptls.cpp:49-78)
+    if (mat_nee(type) && S.num_lights > 0) {
+        float r = rng.next();
+        // LightSampler::sampleLight: lower_bound over the CDF
+        int lo = 0, hi = S.num_lights;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (__ldg(&S.light_cdf[mid]) < r) lo = mid + 1; else hi = mid;
+        }
+        int li = lo < S.num_lights ? lo : S.num_lights - 1;
+        const float4* L = S.lights + 6 * li;
+        float4 l0 = __ldg(&L[0]), l1 = __ldg(&L[1]), l2 = __ldg(&L[2]);
+        float4 n0 = __ldg(&L[3]), n1 = __ldg(&L[4]), n2 = __ldg(&L[5]);
+        // Triangle::sample (src/scene/triangle.cpp:45-55)
+        float r1 = rng.next();
+        float r2 = rng.next();
+        if (r1 + r2 > 1.f) { r1 = 1.f - r1; r2 = 1.f - r2; }
+        float lw = 1.f - r1 - r2;
+        f3 light_pos = lw * xyz(l0) + r1 * xyz(l1) + r2 * xyz(l2);
+        f3 light_normal = normalized(lw * xyz(n0) + r1 * xyz(n1) + r2 * xyz(n2));
+        f3 light_vec = light_pos - hit_pos;
+        f3 wl = normalized(light_vec);
+        f3 Ke = mk(l0.w, l1.w, l2.w);
+        float light_pdf = S.light_p;
+        float cos_l = dot(light_normal, -wl);
+        float light_omega_pdf = light_pdf * dot(light_vec, light_vec) / smax(1e-6f, cos_l);
+        float brdf_omega_pdf = mat_pdf(M, wo, normal, wl);
+        float mis = light_omega_pdf / (light_omega_pdf + brdf_omega_pdf);
+        if (!pol.mis) mis = 0.5f;
+        fac = 1.0f - mis;
+        f3 brdf = mat_bxdf(M, wo, normal, wl);
+        f3 Ll = Ke / norm2(light_vec) * smax(0.f, cos_l) / light_pdf;
+        f3 c = Ll * brdf * smax(0.f, dot(normal, normalized(light_pos - hit_pos))) * mis;
+        c = c * T;
+        if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
+            // Visible iff the closest t satisfies t + 2e-3 > |light_vec| (in
+            // double there), i.e. occluded iff some hit has t <= |lv| - 2e-3.
+            double lim = (double)norm(light_vec) - 2e-3;
+            float tmax = lim > 0.0 ? __double2float_rd(lim) : 0.0f;
+            if (tmax > 0.f) {
+                int q = warp_append(true, &P.counters[CNT_SHADOW]);
+                f3 so = hit_pos + wl * 1e-3f;
+                P.sh_o[q] = make_float4(so.x, so.y, so.z, tmax);
+                P.sh_d[q] = make_float4(wl.x, wl.y, wl.z, __int_as_float(slot));
+                P.sh_c[q] = make_float4(c.x, c.y, c.z, 0.f);
+            } else {  // no hit with t > 0 can be that close: always visible
+                float4 r = P.rad[slot];
+                P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+            }
+        }
+    }
+    if (pol.maxdepth > 0 && depth + 1 >= pol.maxdepth) return;
+    // Russian roulette (rendererptls.cpp:80-83)
+    float prr = depth < pol.rrdepth ? 1.0f : pol.prr;
+    float u = rng.next();
+    if (depth >= pol.rrdepth && u > prr) return;
+    f3 wi = mat_sample(M, rng, wo, normal);
+    float pdf = mat_pdf(M, wo, normal, wi);
+    f3 brdf = mat_bxdf(M, wo, normal, wi);
+    // contri = Li * |wi.n| * brdf / pdf / prr (rendererptls.cpp:90)
+    f3 Tn = T * fabsf(dot(wi, normal)) * brdf / pdf / prr;
+    f3 no = hit_pos + wi * 1e-3f;
+    int q = warp_append(true, &P.counters[CNT_OUT]);
+    P.queue_out[q] = slot;
+    P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
+    P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
+    P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
+    P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, meta.w + 1u);
+}
+
+// Shades the bucketed queue: categories are contiguous, so each warp mostly
+// runs one material's code.
+__global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Policy pol, int capacity) {
+    uint32_t cnt[NUM_CAT], start[NUM_CAT];
+    uint32_t total = 0;
+#pragma unroll
+    for (int c = 0; c < NUM_CAT; ++c) { cnt[c] = P.counters[CNT_CAT + c]; start[c] = total; total += cnt[c]; }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        int c = 0;
+#pragma unroll
+        for (int k = 1; k < NUM_CAT; ++k) if (i >= start[k]) c = k;
+        int slot = P.sorted[(size_t)c * capacity + (i - start[c])];
+        shade_one(P, S, pol, slot);
+    }
+}
+
+// ---------------------------------------------------------------- shadow rays
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_shadow(PathState P, DeviceScene S) {
+    const uint32_t n = P.counters[CNT_SHADOW];
+    const int lane = threadIdx.x & 31;
+    uint32_t nv = 0, nt = 0;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK_SH], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t idx = base + lane;
+        if (idx < n) {
+            float4 o = P.sh_o[idx], d = P.sh_d[idx];
+            if (!any_hit(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr, COUNT ? &nt : nullptr)) {
+                int slot = __float_as_int(d.w);
+                float4 c = P.sh_c[idx];
+                float4 r = P.rad[slot];
+                P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+            }
+        }
+    }
+    if (COUNT) {
+        warp_count(nv, &P.counters[CNT_SH_NODES]);
+        warp_count(nt, &P.counters[CNT_SH_TRIS]);
+    }
+}
+
+// Moves the continuation queue into place for the next bounce and clears the
+// per-bounce counters; also keeps the 64-bit ray totals.
+__global__ void k_advance(uint32_t* counters) {
+    uint32_t in = counters[CNT_IN], sh = counters[CNT_SHADOW];
+    unsigned long long* rays = reinterpret_cast<unsigned long long*>(counters + CNT_RAYS);
+    unsigned long long* shr = reinterpret_cast<unsigned long long*>(counters + CNT_SHRAYS);
+    *rays += in;
+    *shr += sh;
+    counters[CNT_IN] = counters[CNT_OUT];
+    counters[CNT_OUT] = 0;
+    counters[CNT_SHADOW] = 0;
+    counters[CNT_WORK] = 0;
+    counters[CNT_WORK_SH] = 0;
+    for (int c = 0; c < NUM_CAT; ++c) counters[CNT_CAT + c] = 0;
+}
+
+// Clears the per-wave counters; the error word and the totals from
+// CNT_RAYS on are kept for the whole render.
+__global__ void k_reset_counters(uint32_t* counters) {
+    int i = threadIdx.x;
+    if (i < CNT_RAYS && i != CNT_ERR) counters[i] = 0;
+}
+
+// ---------------------------------------------------------------- film
+// For every pixel of the wave, adds max(0, L) of its samples in sample order
+// (rendererptls.cpp:173). film holds npix float4 sums.
+__global__ void k_film(PathState P, WaveDesc W, float4* film) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)W.npix) return;
+    uint64_t end = W.base + (uint64_t)W.count;
+    uint64_t s_first = W.base / (uint64_t)W.npix;
+    uint64_t g = s_first * (uint64_t)W.npix + p;
+    if (g < W.base) g += (uint64_t)W.npix;
+    if (g >= end) return;
+    float4 acc = film[p];
+    for (; g < end; g += (uint64_t)W.npix) {
+        float4 r = P.rad[g - W.base];
+        acc.x += smax(0.f, r.x);
+        acc.y += smax(0.f, r.y);
+        acc.z += smax(0.f, r.z);
+    }
+    film[p] = acc;
+}
+
+// Copies per-sample max(0, L) to out[(pixel * spp + sample) * 3].
+__global__ void k_collect(PathState P, WaveDesc W, float* out, int spp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W.count) return;
+    uint64_t g = W.base + (uint64_t)i;
+    uint64_t srel = g / (uint64_t)W.npix, pidx = g % (uint64_t)W.npix;
+    float4 r = P.rad[i];
+    float* o = out + (pidx * (uint64_t)spp + srel) * 3;
+    o[0] = smax(0.f, r.x); o[1] = smax(0.f, r.y); o[2] = smax(0.f, r.z);
+}
+
+// Mean, gamma and 8-bit conversion (rendererptls.cpp:175-180).
+__global__ void k_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    float4 a = film[p];
+    float m[3] = {a.x * inv_spp, a.y * inv_spp, a.z * inv_spp};
+    for (int k = 0; k < 3; ++k) {
+        if (hdr) hdr[3 * p + k] = m[k];
+        if (rgb8) {
+            float g = powf(m[k], (float)(1.0 / 2.2)) * 255.0f;
+            g = smin(255.0f, smax(0.0f, g));
+            rgb8[3 * p + k] = (uint8_t)(int)g;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- single queries
+__global__ void k_intersect(DeviceScene S, int n, const float* o, const float* d, int* tri, float* t, float* b1,
+                            float* b2, uint32_t* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float tt, u, v;
+    int k = closest_hit(S, mk(o[3 * i], o[3 * i + 1], o[3 * i + 2]), mk(d[3 * i], d[3 * i + 1], d[3 * i + 2]), tt, u, v, err);
+    tri[i] = k >= 0 ? __float_as_int(__ldg(&S.tri_geo[3 * k]).w) : -1;
+    t[i] = tt; b1[i] = u; b2[i] = v;
+}
+
+struct ListRng {
+    const float* u;
+    int i;
+    __device__ float next() { return i < 4 ? u[i++] : 0.5f; }
+};
+
+__global__ void k_material_probe(DeviceScene S, int mat, int n, const float* wo, const float* nrm, const float* wi,
+                                 const float* uv, const float* u, float* f, float* pdf, float* wi_s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 a = mk(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), nn = mk(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+    f3 b = mk(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+    MatView M = load_mat(S, mat, mk(uv[3 * i], uv[3 * i + 1], uv[3 * i + 2]));
+    f3 ff = mat_bxdf(M, a, nn, b);
+    pdf[i] = mat_pdf(M, a, nn, b);
+    ListRng r{u + 4 * i, 0};
+    f3 ws = mat_sample(M, r, a, nn);
+    f[3 * i] = ff.x; f[3 * i + 1] = ff.y; f[3 * i + 2] = ff.z;
+    wi_s[3 * i] = ws.x; wi_s[3 * i + 1] = ws.y; wi_s[3 * i + 2] = ws.z;
+}
+
+// ---------------------------------------------------------------- launchers
+static int g_trace_blocks = 0, g_shadow_blocks = 0;
+
+void launch_setup(int num_sms) {
+    int b1 = 0, b2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_trace<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_shadow<false>, 128, 0);
+    g_trace_blocks = num_sms * (b1 > 0 ? b1 : 1);
+    g_shadow_blocks = num_sms * (b2 > 0 ? b2 : 1);
+}
+
+void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
+                   cudaStream_t st) {
+    k_raygen<<<(W.count + 255) / 256, 256, 0, st>>>(P, W, cam, film_h, pol);
+}
+
+void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
+                   cudaStream_t st, cudaEvent_t* ev, bool count) {
+    if (ev) cudaEventRecord(ev[0], st);
+    if (count) k_trace<true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
+    else k_trace<false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
+    if (ev) cudaEventRecord(ev[1], st);
+    int shade_blocks = (max_count + 127) / 128;
+    if (shade_blocks < 1) shade_blocks = 1;
+    k_shade<<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity);
+    if (ev) cudaEventRecord(ev[2], st);
+    if (count) k_shadow<true><<<g_shadow_blocks, 128, 0, st>>>(P, S);
+    else k_shadow<false><<<g_shadow_blocks, 128, 0, st>>>(P, S);
+    if (ev) cudaEventRecord(ev[3], st);
+    k_advance<<<1, 1, 0, st>>>(P.counters);
+}
+
+void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, 32, 0, st>>>(counters); }
+
+void launch_film(const PathState& P, const WaveDesc& W, float4* film, cudaStream_t st) {
+    k_film<<<(W.npix + 255) / 256, 256, 0, st>>>(P, W, film);
+}
+
+void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st) {
+    k_collect<<<(W.count + 255) / 256, 256, 0, st>>>(P, W, out, spp);
+}
+
+void launch_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8, cudaStream_t st) {
+    k_finish<<<(npix + 255) / 256, 256, 0, st>>>(film, npix, inv_spp, hdr, rgb8);
+}
+
+void launch_intersect(const DeviceScene& S, int n, const float* o, const float* d, int* tri, float* t, float* b1,
+                      float* b2, uint32_t* err, cudaStream_t st) {
+    k_intersect<<<(n + 127) / 128, 128, 0, st>>>(S, n, o, d, tri, t, b1, b2, err);
+}
+
+void launch_material_probe(const DeviceScene& S, int mat, int n, const float* wo, const float* nrm, const float* wi,
+                           const float* uv, const float* u, float* f, float* pdf, float* wi_s, cudaStream_t st) {
+    k_material_probe<<<(n + 127) / 128, 128, 0, st>>>(S, mat, n, wo, nrm, wi, uv, u, f, pdf, wi_s);
+}
+
+}  // namespace nr

@@ -1,0 +1,32 @@
+// Launchers of the ptnee wavefront kernels (integrator.cu).
+#pragma once
+#include "nr_types.h"
+
+namespace nr {
+
+// One wavefront batch: global path indices [base, base + count) with
+// g = (sample - sample0) * npix + pixel_index.
+struct WaveDesc {
+    uint64_t base;
+    int32_t count;
+    int32_t npix;
+    uint32_t sample0;
+    const int32_t* pix_xy;  // device (x, y) list, or null for the full frame
+};
+
+void launch_setup(int num_sms);
+void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
+                   cudaStream_t st);
+// trace + sort, shade, shadow, advance. ev (optional) receives 4 events.
+void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
+                   cudaStream_t st, cudaEvent_t* ev, bool count);
+void launch_reset_counters(uint32_t* counters, cudaStream_t st);
+void launch_film(const PathState& P, const WaveDesc& W, float4* film, cudaStream_t st);
+void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st);
+void launch_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8, cudaStream_t st);
+void launch_intersect(const DeviceScene& S, int n, const float* o, const float* d, int* tri, float* t, float* b1,
+                      float* b2, uint32_t* err, cudaStream_t st);
+void launch_material_probe(const DeviceScene& S, int mat, int n, const float* wo, const float* nrm, const float* wi,
+                           const float* uv, const float* u, float* f, float* pdf, float* wi_s, cudaStream_t st);
+
+}  // namespace nr

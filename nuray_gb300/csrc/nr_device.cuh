@@ -1,0 +1,293 @@
+// Device building blocks of the ptnee wavefront: vector helpers, the Philox
+// path stream, the reference-exact ray/box and ray/triangle tests and the
+// BVH traversals. Included by the .cu files of libnuray_gpu.so only.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "nr_types.h"
+
+namespace nr {
+
+// ------------------------------------------------------------------ vectors
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 mk(float s) { return {s, s, s}; }
+__device__ __forceinline__ f3 xyz(float4 v) { return {v.x, v.y, v.z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float norm2(f3 a) { return dot(a, a); }
+__device__ __forceinline__ float norm(f3 a) { return sqrtf(norm2(a)); }
+// vec3::normalized divides by |a| + 1e-8 (src/math/vec3.cpp:70-73)
+__device__ __forceinline__ f3 normalized(f3 a) { return a / (norm(a) + 1e-8f); }
+// std::max / std::min semantics (first argument kept unless strictly beaten)
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+
+// Rounded-to-nearest float ops that the compiler may not fuse; used where the
+// reference's FP32 results have to be reproduced bit for bit.
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ f3 rsub3(f3 a, f3 b) { return {rsub(a.x, b.x), rsub(a.y, b.y), rsub(a.z, b.z)}; }
+__device__ __forceinline__ float rdot(f3 a, f3 b) { return radd(radd(rmul(a.x, b.x), rmul(a.y, b.y)), rmul(a.z, b.z)); }
+__device__ __forceinline__ f3 rcross(f3 a, f3 b) {
+    return {rsub(rmul(a.y, b.z), rmul(a.z, b.y)), rsub(rmul(a.z, b.x), rmul(a.x, b.z)),
+            rsub(rmul(a.x, b.y), rmul(a.y, b.x))};
+}
+
+// Correctly rounded a / b given rb = RN(1/b): one residual correction of
+// the product a * rb (Markstein). Exact for finite, non-denormal results.
+__device__ __forceinline__ float qdiv(float a, float b, float rb) {
+    float q0 = __fmul_rn(a, rb);
+    float r = __fmaf_rn(-q0, b, a);
+    return __fmaf_rn(r, rb, q0);
+}
+
+// RN_float(x + 1e-6) where 1e-6 is the double literal of the reference's
+// `s1.dot(e1) + 1e-6` (src/scene/triangle.cpp:31): a float TwoSum with the
+// split constant hi + lo. Differs from the double evaluation only when the
+// exact sum lies within 2^-48 of a float rounding boundary.
+__device__ __forceinline__ float add_1e6(float x) {
+    const float hi = 9.99999997475242708e-07f;
+    const float lo = (float)(1e-6 - (double)9.99999997475242708e-07f);
+    float s = __fadd_rn(x, hi);
+    float bb = __fsub_rn(s, x);
+    float e = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(hi, bb));
+    return __fadd_rn(s, __fadd_rn(e, lo));
+}
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon et al., SC'11). Path stream: draw n of path
+// (pixel, sample) is lane n%4 of philox(ctr = (pixel, sample, n/4, tag),
+// key = seed); uniform = (x >> 8) * 2^-24.
+#define NR_STREAM_TAG 0x6e755279u
+__device__ __forceinline__ uint4 philox10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+struct Stream {
+    uint2 key;
+    uint32_t pixel, sample, n;
+    uint4 buf;
+    __device__ __forceinline__ void init(uint32_t seed_lo, uint32_t seed_hi, uint32_t px, uint32_t smp, uint32_t first) {
+        key = make_uint2(seed_lo, seed_hi);
+        pixel = px; sample = smp; n = first;
+        buf = philox10(make_uint4(pixel, sample, n >> 2, NR_STREAM_TAG), key);
+    }
+    __device__ __forceinline__ float next() {
+        if ((n & 3u) == 0u && n != 0u) buf = philox10(make_uint4(pixel, sample, n >> 2, NR_STREAM_TAG), key);
+        uint32_t lane = n & 3u;
+        uint32_t x = lane == 0 ? buf.x : (lane == 1 ? buf.y : (lane == 2 ? buf.z : buf.w));
+        ++n;
+        return (float)(x >> 8) * (1.0f / 16777216.0f);
+    }
+};
+
+// ------------------------------------------------------------------ intersection
+// Ray prepared for the exact slab test: denominators d + 1e-9f and their
+// correctly rounded reciprocals (src/hierarchy/bvhnode.cpp:41).
+struct SlabRay {
+    float ox, oy, oz;
+    float dx, dy, dz;     // d + 1e-9f
+    float rx, ry, rz;     // RN(1 / (d + 1e-9f))
+};
+__device__ __forceinline__ SlabRay make_slab_ray(f3 o, f3 d) {
+    SlabRay r;
+    r.ox = o.x; r.oy = o.y; r.oz = o.z;
+    r.dx = __fadd_rn(d.x, 1e-9f); r.dy = __fadd_rn(d.y, 1e-9f); r.dz = __fadd_rn(d.z, 1e-9f);
+    r.rx = __frcp_rn(r.dx); r.ry = __frcp_rn(r.dy); r.rz = __frcp_rn(r.dz);
+    return r;
+}
+
+// BVHNode::intersect (src/hierarchy/bvhnode.cpp:35-48) with the same
+// rounding: t = (bound - o) / (d + 1e-9f), swap, std::max / std::min.
+// Returns the entry distance in *tin when accepted.
+__device__ __forceinline__ bool slab_axis(float lo, float hi, float o, float d, float rd, float& tin, float& tout) {
+    float t1 = qdiv(__fsub_rn(lo, o), d, rd);
+    float t2 = qdiv(__fsub_rn(hi, o), d, rd);
+    if (t1 > t2) { float s = t1; t1 = t2; t2 = s; }
+    tin = smax(tin, t1);
+    tout = smin(tout, t2);
+    return true;
+}
+__device__ __forceinline__ bool box_test(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                         float& t_entry) {
+    float tin = -1e18f, tout = 1e18f;
+    slab_axis(lx, hx, r.ox, r.dx, r.rx, tin, tout);
+    slab_axis(ly, hy, r.oy, r.dy, r.ry, tin, tout);
+    slab_axis(lz, hz, r.oz, r.dz, r.rz, tin, tout);
+    t_entry = tin;
+    return tin <= tout && tout >= 0.0f;
+}
+
+// Triangle::intersection (src/scene/triangle.cpp:27-33) followed by the leaf
+// acceptance test of BVHNode::getIntersection (src/hierarchy/bvhnode.cpp:55-63):
+// t < limit && t > 0 && b1 >= 0 && b2 >= 0 && b1 + b2 <= 1.
+__device__ __forceinline__ bool tri_test(f3 o, f3 d, float4 g0, float4 g1, float4 g2, float limit, float& t, float& b1,
+                                         float& b2) {
+    f3 p0 = xyz(g0), e1 = xyz(g1), e2 = xyz(g2);
+    f3 s = rsub3(o, p0);
+    f3 s1 = rcross(d, e2);
+    f3 s2 = rcross(s, e1);
+    float tt = rdot(s2, e2);
+    float q = add_1e6(rdot(s1, e1));
+    // t = tt / q > 0 needs equal signs and tt != 0; anything else is rejected.
+    if (tt == 0.0f || ((__float_as_uint(tt) ^ __float_as_uint(q)) & 0x80000000u)) return false;
+    float rq = __frcp_rn(q);
+    t = qdiv(tt, q, rq);
+    if (!(t < limit && t > 0.0f)) return false;
+    b1 = qdiv(rdot(s1, s), q, rq);
+    b2 = qdiv(rdot(s2, d), q, rq);
+    return b1 >= 0.0f && b2 >= 0.0f && __fadd_rn(b1, b2) <= 1.0f;
+}
+
+// Pruning margin: a subtree whose entry distance exceeds the best hit by
+// more than this relative amount is skipped. The reference's biased
+// determinant (q + 1e-6) shortens t by a factor q / (q + 1e-6), so a
+// triangle can report a t slightly below its box's entry distance; the
+// margin keeps such triangles reachable unless |q| < 1e-6 / margin.
+#define NR_PRUNE_MARGIN 1e-3f
+#define NR_STACK NR_STACK_LIMIT
+
+// Closest hit with the reference's exhaustive semantics (BVH::_traversal,
+// src/hierarchy/bvh.cpp:99-127): the minimum t over reachable triangles;
+// equal t resolved towards the later leaf in depth-first order (the
+// reference keeps the right subtree unless the left is strictly nearer) and,
+// within a leaf, towards the earlier triangle. Visits children near-first
+// and prunes with the margin above. Returns the flattened triangle index or
+// -1; err is set on a stack overflow.
+__device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, float& best_t, float& best_b1,
+                                           float& best_b2, uint32_t* err, uint32_t* nodes_visited = nullptr,
+                                           uint32_t* tris_tested = nullptr) {
+    best_t = 1e18f; best_b1 = 0.f; best_b2 = 0.f;
+    int best = -1, best_leaf = -1;
+    if (S.root_ref == INT32_MIN) return -1;
+    SlabRay R = make_slab_ray(o, d);
+    float te;
+    if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return -1;
+    int stack[NR_STACK];
+    float stack_t[NR_STACK];
+    int sp = 0;
+    int ref = S.root_ref;
+    uint32_t nv = 0, nt = 0;
+    while (true) {
+        if (ref >= 0) {
+            const GpuNode& N = S.nodes[ref];
+            float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
+            int4 k = __ldg(&N.d);
+            ++nv;
+            float t0, t1;
+            bool h0 = box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
+            bool h1 = box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
+            float lim = best_t * (1.0f + NR_PRUNE_MARGIN);
+            h0 = h0 && t0 <= lim;
+            h1 = h1 && t1 <= lim;
+            if (h0 && h1) {
+                int nr = k.x, fr = k.y;
+                float ft = t1;
+                if (t1 < t0) { nr = k.y; fr = k.x; ft = t0; }
+                if (sp >= NR_STACK) { atomicOr(err, 1u); break; }
+                stack[sp] = fr; stack_t[sp] = ft; ++sp;
+                ref = nr;
+                continue;
+            }
+            if (h0) { ref = k.x; continue; }
+            if (h1) { ref = k.y; continue; }
+        } else {
+            int first = leaf_first(ref), cnt = leaf_count(ref);
+            float lt = 1e18f, lb1 = 0.f, lb2 = 0.f;
+            int li = -1;
+            for (int i = 0; i < cnt; ++i) {
+                int ti = first + i;
+                float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
+                ++nt;
+                float t, u, v;
+                if (tri_test(o, d, g0, g1, g2, lt, t, u, v)) { lt = t; lb1 = u; lb2 = v; li = ti; }
+            }
+            if (li >= 0 && (lt < best_t || (lt == best_t && first > best_leaf))) {
+                best_t = lt; best_b1 = lb1; best_b2 = lb2; best = li; best_leaf = first;
+            }
+        }
+        // pop the next subtree that can still hold a hit
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= best_t * (1.0f + NR_PRUNE_MARGIN)) { ref = stack[sp]; found = true; break; }
+        }
+        if (!found) break;
+    }
+    if (nodes_visited) *nodes_visited += nv;
+    if (tris_tested) *tris_tested += nt;
+    return best;
+}
+
+// Shadow query: true when some reachable triangle has a reference hit with
+// t <= tmax (the complement of `t + 2e-3 > |light_vec|` of
+// src/renderer/rendererptls.cpp:71 for the closest hit).
+__device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float tmax, uint32_t* err,
+                                        uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr) {
+    if (S.root_ref == INT32_MIN) return false;
+    SlabRay R = make_slab_ray(o, d);
+    float te;
+    if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return false;
+    const float lim = tmax * (1.0f + NR_PRUNE_MARGIN);
+    int stack[NR_STACK];
+    int sp = 0;
+    int ref = S.root_ref;
+    const float limit = fminf(1e18f, __uint_as_float(__float_as_uint(tmax) + 1u));  // accepts t <= tmax
+    while (true) {
+        if (ref >= 0) {
+            const GpuNode& N = S.nodes[ref];
+            float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
+            int4 k = __ldg(&N.d);
+            if (nodes_visited) ++*nodes_visited;
+            float t0, t1;
+            bool h0 = box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) && t0 <= lim;
+            bool h1 = box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) && t1 <= lim;
+            if (h0 && h1) {
+                int nr = k.x, fr = k.y;
+                if (t1 < t0) { nr = k.y; fr = k.x; }
+                if (sp >= NR_STACK) { atomicOr(err, 1u); return false; }
+                stack[sp++] = fr;
+                ref = nr;
+                continue;
+            }
+            if (h0) { ref = k.x; continue; }
+            if (h1) { ref = k.y; continue; }
+        } else {
+            int first = leaf_first(ref), cnt = leaf_count(ref);
+            for (int i = 0; i < cnt; ++i) {
+                int ti = first + i;
+                float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
+                if (tris_tested) ++*tris_tested;
+                float t, u, v;
+                if (tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
+            }
+        }
+        if (sp == 0) break;
+        ref = stack[--sp];
+    }
+    return false;
+}
+
+}  // namespace nr

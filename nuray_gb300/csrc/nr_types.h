@@ -1,0 +1,108 @@
+// Device-side scene and wavefront layouts shared by the host code and the
+// CUDA kernels of libnuray_gpu.so.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "../../include/nuray.h"
+
+// Entries of the per-thread traversal stack; scenes whose BVH is deeper are
+// rejected at creation.
+#define NR_STACK_LIMIT 96
+
+namespace nr {
+
+// BVH child reference: >= 0 is an internal node index, < 0 a leaf
+// -1 - ((first << 3) | count) with `first` into the flattened triangle
+// arrays (leaves laid out in depth-first order) and count <= 5.
+__host__ __device__ inline int32_t leaf_ref(int32_t first, int32_t count) { return -1 - ((first << 3) | count); }
+__host__ __device__ inline int32_t leaf_first(int32_t ref) { return (-1 - ref) >> 3; }
+__host__ __device__ inline int32_t leaf_count(int32_t ref) { return (-1 - ref) & 7; }
+
+// Internal BVH node, 64 bytes: both children's boxes and references.
+//   a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   d = (ref0, ref1, depth, 0) as int bits
+struct alignas(16) GpuNode {
+    float4 a, b, c;
+    int4 d;
+};
+
+// Per flattened triangle, traversal data, 48 bytes:
+//   g0 = (p0.xyz, loader index bits), g1 = (e1.xyz, material bits), g2 = (e2.xyz, 0)
+// with e1 = p1 - p0 and e2 = p2 - p0 rounded exactly as the reference does.
+// Shading data, 64 bytes:
+//   s0 = (n0.xyz, t0.x), s1 = (n1.xyz, t0.y), s2 = (n2.xyz, t1.x), s3 = (t1.y, t2.x, t2.y, material bits)
+struct DeviceScene {
+    const GpuNode* nodes;
+    const float4* tri_geo;    // 3 per triangle
+    const float4* tri_shade;  // 4 per triangle
+    const nr_material* mats;
+    const float4* tex_texels;
+    const int4* tex_info;     // (w, h, texel offset, 0)
+    const float4* lights;     // 6 per emitter: (p0, Ke.x) (p1, Ke.y) (p2, Ke.z) (n0,0) (n1,0) (n2,0)
+    const float* light_cdf;
+    int32_t num_lights;
+    float light_p;            // LightSampler::p()
+    int32_t root_ref;         // root as a child reference; INT32_MIN for an empty scene
+    float root_lo[3], root_hi[3];
+    int32_t num_tris;
+    int32_t num_mats;
+    int32_t env_tex;
+    float env_gain;
+    int32_t max_depth;        // deepest leaf (root = 0)
+};
+
+// Render policy decoded from the parameter string.
+struct Policy {
+    float prr;        // survival probability (reference key prr, default 0.8)
+    int32_t mis;      // reference key mis (default 1)
+    int32_t rrdepth;  // RR applies at vertex index >= rrdepth (0 = reference)
+    int32_t maxdepth; // 0 = unbounded (reference)
+    uint32_t seed_lo, seed_hi;
+    int32_t imgw, imgh;
+};
+
+// Wavefront path state, structure of arrays, one slot per in-flight path.
+struct PathState {
+    float4* ray_o;   // (origin, unused)
+    float4* ray_d;   // (direction, unused)
+    float4* hit;     // (t, b1, b2, flattened triangle bits or -1)
+    float4* thr;     // (throughput, light_fac)
+    float4* rad;     // (radiance, unused)
+    uint4* meta;     // (pixel, sample, draws taken, vertex depth)
+    // queues of slot indices
+    int32_t* queue_in;
+    int32_t* queue_out;
+    int32_t* sorted;      // slots bucketed by shading category
+    // shadow rays
+    float4* sh_o;    // (origin, t limit)
+    float4* sh_d;    // (direction, slot bits)
+    float4* sh_c;    // (contribution if unoccluded, unused)
+    // device counters (see Counter)
+    uint32_t* counters;
+};
+
+// Shading categories for the material sort: one per material type, then
+// rays that left the scene.
+enum { CAT_MISS = 6, NUM_CAT = 7 };
+
+enum Counter {
+    CNT_IN = 0,        // live paths in queue_in
+    CNT_OUT = 1,       // continuing paths appended to queue_out
+    CNT_SHADOW = 2,    // shadow rays appended
+    CNT_WORK = 3,      // persistent-kernel work cursor (closest hit)
+    CNT_WORK_SH = 4,   // persistent-kernel work cursor (shadow)
+    CNT_CAT = 8,       // 8..14: per-category counts
+    CNT_ERR = 16,      // internal error word (stack overflow etc.), 0 = fine
+    CNT_RAYS = 18,     // 64-bit totals (lo, hi): extension rays,
+    CNT_SHRAYS = 20,   // shadow rays,
+    CNT_NODES = 22,    // BVH nodes visited by closest-hit rays (instrumented runs),
+    CNT_TRIS = 24,     // triangles tested by closest-hit rays,
+    CNT_SH_NODES = 26, // nodes visited by shadow rays,
+    CNT_SH_TRIS = 28,  // triangles tested by shadow rays
+    NUM_COUNTERS = 32
+};
+
+}  // namespace nr

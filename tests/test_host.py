@@ -1,0 +1,132 @@
+"""Host-side logic without a GPU: the C ABI exports, the parameter grammar,
+the loader and the reference-identical BVH builder (through tests/host_shim.cpp)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import shim
+from conftest import ROOT, golden
+from nuray_gb300 import scenes
+
+
+@pytest.fixture(scope="module")
+def host():
+    return shim.load()
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "nuray.h")).read()
+    return sorted(set(re.findall(r"^int (nr_\w+)\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from nuray_gb300 import build
+    path = build.build()
+    L = ctypes.CDLL(path)
+    names = declared_functions()
+    assert len(names) >= 13
+    for n in names:
+        assert hasattr(L, n), n
+    from nuray_gb300._lib import SIGNATURES
+    assert sorted(SIGNATURES) == names
+
+
+def test_library_without_gpu_reports_errors():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from nuray_gb300 import NuRayError, Scene
+    with pytest.raises(NuRayError):
+        Scene.from_arrays(np.zeros((1, 9), np.float32), np.zeros(1, np.int32), [dict(type=0, c0=(1, 1, 1))])
+
+
+def test_config_grammar(host):
+    p = b"renderer=ptnee imgw=320 spp=abc campos=0,120,200 bad=1,2 prr=0.5 k=v=w"
+    assert host.shim_config_int(p, b"imgw", 1) == 320
+    assert host.shim_config_int(p, b"spp", 7) == 7        # unparsable -> default
+    assert host.shim_config_int(p, b"missing", 9) == 9
+    assert abs(host.shim_config_float(p, b"prr", 0.8) - 0.5) < 1e-7
+    v = np.zeros(3, np.float32)
+    assert host.shim_config_vec3(p, b"campos", v.ctypes.data) == 1 and list(v) == [0, 120, 200]
+    assert host.shim_config_vec3(p, b"bad", v.ctypes.data) == 0
+
+
+def test_camera_matches_oracle(host, port_lib):
+    from nuray_gb300._lib import Camera
+    from oracle.bind import Oracle
+    g = golden("cornell_intersect.npz")
+    cam, fh = Camera(), ctypes.c_float()
+    params = b"imgw=320 imgh=240 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
+    host.shim_camera(params, ctypes.byref(cam), ctypes.byref(fh))
+    assert list(cam.pos) == [0, 120, 200]
+    np.testing.assert_allclose(list(cam.gaze), [0, 0, -1], atol=1e-6)
+    np.testing.assert_allclose(fh.value, 2 * np.tan(64 * 3.14159 / 360), rtol=1e-6)
+    cam2 = Camera()
+    host.shim_camera(b"cameuler=30,-20,10", ctypes.byref(cam2), ctypes.byref(fh))
+    assert abs(np.linalg.norm(list(cam2.gaze)) - 1) < 1e-5
+
+
+def test_bvh_builder_matches_reference_tree(host):
+    g = golden("cornell_bvh.npz")
+    sc = golden("cornell_scene.npz")
+    box, kids, first, count, tris, depth = shim.bvh(host, sc["pos"])
+    for a, k in zip((box, kids, first, count, tris), ("box", "kids", "first", "count", "tris")):
+        np.testing.assert_array_equal(a, g[k])
+    s = golden("small_ref.npz")
+    small = scenes.small_scene()
+    res = shim.bvh(host, small["pos"])
+    for a, k in zip(res[:5], ("box", "kids", "first", "count", "tris")):
+        np.testing.assert_array_equal(a, s[k])
+
+
+def test_bvh_builder_parallel_is_deterministic(host, port_lib):
+    from oracle.bind import Oracle
+    sc = scenes.terrain_spheres(3, tiles=16, cells_per_tile=8, spheres=64, slices=16, stacks=12, lights=8,
+                                n_mats=8, extent=64.0)
+    one = shim.bvh(host, sc["pos"], threads=1)
+    many = shim.bvh(host, sc["pos"], threads=8)
+    port = Oracle("port", sc).bvh()
+    for a, b, c in zip(one[:5], many[:5], port):
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(a, c)
+    assert one[2][one[1][:, 0] < 0].min() >= 0 and one[3].max() <= 5
+
+
+def test_loader_matches_reference_loader_fixture(host):
+    ref = "/root/reference/scenes/cornell/CornellBox-Original.obj"
+    if not os.path.exists(ref):
+        pytest.skip("reference scenes not present")
+    pos, uv, nrm, mat, mats = shim.load_scene(host, ref + " -s 100\n")
+    g = golden("cornell_scene.npz")
+    np.testing.assert_array_equal(pos, g["pos"])
+    np.testing.assert_array_equal(uv, g["uv"])
+    np.testing.assert_array_equal(nrm, g["nrm"])
+    # materials: compare contents per triangle (the indices follow creation order)
+    for i in range(len(mat)):
+        m = mats[mat[i]]
+        gi, gf = g["mat_i"][g["mat"][i]], g["mat_f"][g["mat"][i]]
+        assert m.type == gi[0]
+        np.testing.assert_array_equal(list(m.c0), gf[0:3])
+
+
+def test_loader_forced_materials_and_errors(host, tmp_path):
+    obj = tmp_path / "q.obj"
+    obj.write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 1 1\nf 1/1 2/2 3/3 4\nf -4 -3 -2\n")
+    pos, uv, nrm, mat, mats = shim.load_scene(host, f"{obj} -p 1 2 3 -s 2 -m=ggxr 0.5 0.6 0.7 0.3\n"
+                                                    f"{obj} -m=light 1 2 3\n{obj} -m=ggx 1 1 1 0.2 1.5 -m=glass 1 1 1 1.4\n")
+    assert pos.shape[0] == 9  # quad -> 2 triangles + 1, three lines
+    np.testing.assert_array_equal(pos[0, :3], [1, 2, 3])
+    np.testing.assert_array_equal(pos[0, 3:6], [3, 2, 3])
+    assert [m.type for m in mats] == [1, 5, 2, 3]  # later -m flags replace earlier ones, glass last
+    assert abs(mats[0].alpha - 0.3) < 1e-7 and abs(mats[3].ior - 1.4) < 1e-6
+    np.testing.assert_allclose(nrm[0, :3], [0, 0, 1], atol=1e-6)  # face normal when no vn
+    np.testing.assert_array_equal(uv[1], [1, 1, 0, 0, 0, 0])      # second half of the quad: vt 3, (none), vt 1
+    with pytest.raises(ValueError, match="cannot open"):
+        shim.load_scene(host, str(tmp_path / "missing.obj") + "\n")
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nf 1 2 3\n")
+    with pytest.raises(ValueError, match="out of range"):
+        shim.load_scene(host, f"{bad} -m=light 1 1 1\n")

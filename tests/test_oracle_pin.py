@@ -1,0 +1,140 @@
+"""Pins the CPU restatement (oracle/port) to the reference.
+
+Against the reference compiled from its own sources (oracle/_ref, where the
+checkout exists) the restatement must agree bit for bit; against the
+committed fixtures (generated from the reference by tests/golden/make_golden.py)
+it must agree bit for bit on x86 and within a few ulps elsewhere (libm
+differences between architectures).
+"""
+import platform
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle.bind import Oracle, pixel_grid
+from nuray_gb300 import scenes
+
+EXACT = platform.machine() in ("x86_64", "AMD64")
+
+
+def _close(a, b, rtol=1e-5, atol=1e-6):
+    if EXACT:
+        np.testing.assert_array_equal(a, b)
+    else:
+        np.testing.assert_allclose(a, b, rtol=rtol, atol=atol)
+
+
+def cornell_scene():
+    g = golden("cornell_scene.npz")
+    mats = []
+    for i, f in zip(g["mat_i"], g["mat_f"]):
+        mats.append(dict(type=int(i[0]), c0=f[0:3].tolist(), c1=f[3:6].tolist(), alpha=float(f[6]), ior=float(f[7]),
+                         ns=float(f[8])))
+    return dict(pos=g["pos"], uv=g["uv"], nrm=g["nrm"], mat=g["mat"], mats=mats, textures=[], env_tex=-1)
+
+
+def test_cornell_fixture_shape():
+    s = cornell_scene()
+    assert s["pos"].shape == (36, 9)  # 18 quads
+    types = [m["type"] for m in s["mats"]]
+    assert types.count(5) == 1  # one emitter material, Ke = (17, 12, 4)
+    light = s["mats"][types.index(5)]
+    assert light["c0"] == [17.0, 12.0, 4.0]
+
+
+def test_port_bvh_matches_golden(port_lib):
+    P = Oracle("port", cornell_scene())
+    g = golden("cornell_bvh.npz")
+    for a, k in zip(P.bvh(), ("box", "kids", "first", "count", "tris")):
+        np.testing.assert_array_equal(a, g[k])
+    s = golden("small_ref.npz")
+    P2 = Oracle("port", scenes.small_scene())
+    for a, k in zip(P2.bvh(), ("box", "kids", "first", "count", "tris")):
+        np.testing.assert_array_equal(a, s[k])
+
+
+def test_port_intersect_matches_golden(port_lib):
+    g = golden("cornell_intersect.npz")
+    P = Oracle("port", cornell_scene())
+    tri, t, b1, b2 = P.intersect(g["o"], g["d"])
+    np.testing.assert_array_equal(tri, g["tri"])
+    _close(t, g["t"])
+    _close(b1, g["b1"])
+    _close(b2, g["b2"])
+    o, d = P.camera_rays("renderer=ptnee imgw=320 imgh=240 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 "
+                         "camasp=1.333", g["fx"], g["fy"])
+    _close(d, g["cam_d"])
+
+
+def test_port_samples_match_golden(port_lib):
+    g = golden("cornell_samples.npz")
+    P = Oracle("port", cornell_scene())
+    rad = P.render_samples(str(g["params"]), g["pix"], 8, seed=0)
+    _close(rad, g["rad"], rtol=1e-4, atol=1e-5)
+    s = golden("small_ref.npz")
+    P2 = Oracle("port", scenes.small_scene())
+    rad2 = P2.render_samples(str(s["params"]), s["pix"], 8, seed=0)
+    _close(rad2, s["rad"], rtol=1e-4, atol=1e-5)
+
+
+def test_port_probes_match_golden(port_lib):
+    s = golden("small_ref.npz")
+    sc = scenes.small_scene()
+    P = Oracle("port", sc)
+    for m in range(len(sc["mats"])):
+        f, pdf, ws = P.material_probe(m, s["wo"], s["nrm"], s["wi"], s["uv"], s["u"])
+        _close(f, s[f"f{m}"], rtol=1e-5)
+        _close(pdf, s[f"pdf{m}"], rtol=1e-5)
+        _close(ws, s[f"ws{m}"], rtol=1e-5)
+    tri, p = P.light_pick(s["light_u"])
+    np.testing.assert_array_equal(tri, s["light_tri"])
+    assert np.float32(p) == s["light_p"]
+    _close(P.texture_lookup(int(s["tex_mat"]), 0, s["tex_uv"]), s["tex_rgb"])
+    _close(P.texture_lookup(0, 1, s["tex_uv"]), s["env_rgb"])
+
+
+# ---- against the reference compiled here (skipped without the checkout)
+
+def test_port_equals_reference_cornell_full(port_lib, ref_lib):
+    import os
+    R = Oracle("ref", desc=os.path.join("/root/reference/scenes/cornell/CornellBox-Original.obj") + " -s 100\n")
+    P = Oracle("port", cornell_scene())
+    params = "renderer=ptnee imgw=80 imgh=60 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
+    pix = pixel_grid(80, 60)
+    np.testing.assert_array_equal(P.render_samples(params, pix, 4, seed=3), R.render_samples(params, pix, 4, seed=3))
+    params_nomis = params + " mis=0 prr=0.6"
+    np.testing.assert_array_equal(P.render_samples(params_nomis, pix, 2, seed=5),
+                                  R.render_samples(params_nomis, pix, 2, seed=5))
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_port_equals_reference_mixed(port_lib, ref_lib, seed):
+    sc = scenes.small_scene(seed)
+    P, R = Oracle("port", sc), Oracle("ref", sc)
+    for a, b in zip(P.bvh(), R.bvh()):
+        np.testing.assert_array_equal(a, b)
+    pix = pixel_grid(48, 32)
+    np.testing.assert_array_equal(P.render_samples(sc["params"], pix, 4, seed=seed),
+                                  R.render_samples(sc["params"], pix, 4, seed=seed))
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-25, 25, size=(5000, 3)).astype(np.float32)
+    d = rng.normal(size=(5000, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    for a, b in zip(P.intersect(o, d), R.intersect(o, d)):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_port_equals_reference_no_lights_and_empty(port_lib, ref_lib):
+    sc = scenes.small_scene(4)
+    # drop the emitters: NEE then finds no light (LightSampler returns nullptr)
+    keep = np.array([sc["mats"][m]["type"] != 5 for m in sc["mat"]])
+    dark = dict(sc, pos=sc["pos"][keep], uv=sc["uv"][keep], nrm=sc["nrm"][keep], mat=sc["mat"][keep])
+    P, R = Oracle("port", dark), Oracle("ref", dark)
+    pix = pixel_grid(48, 32)
+    np.testing.assert_array_equal(P.render_samples(sc["params"], pix, 2), R.render_samples(sc["params"], pix, 2))
+    # a scene of at most five triangles is a single leaf
+    tiny = dict(sc, pos=sc["pos"][:4], uv=sc["uv"][:4], nrm=sc["nrm"][:4], mat=sc["mat"][:4])
+    P, R = Oracle("port", tiny), Oracle("ref", tiny)
+    for a, b in zip(P.bvh(), R.bvh()):
+        np.testing.assert_array_equal(a, b)
