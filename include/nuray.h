@@ -15,6 +15,8 @@
  *                                    + Renderer::prepare (src/renderer/renderer.cpp:30-39)
  *   nr_scene_destroy                 Loader::~Loader / BVH::~BVH (src/scene/loader.cpp:10-16,
  *                                    src/hierarchy/bvh.cpp:76-79)
+ *   nr_scene_set_env                 Renderer::setEnvmap + Envmap(texture, gain)
+ *                                    (src/renderer/renderer.cpp:41-44, src/scene/envmap.cpp:5-24)
  *   nr_intersect                     Renderer::intersect -> BVH::intersection
  *                                    (src/renderer/renderer.cpp:10-28, src/hierarchy/bvh.cpp:129-137)
  *   nr_camera_from_params            Camera(fov, asp, pos, yaw, pitch, roll) as built by Cmd::main
@@ -149,6 +151,12 @@ int nr_scene_create(const nr_scene_desc* desc, nr_scene** out);
 int nr_scene_load(const char* scene_desc, nr_scene** out);
 
 int nr_scene_destroy(nr_scene* scene);
+
+/* Renderer::setEnvmap (src/renderer/renderer.cpp:41-44) together with the
+ * Envmap the CLI builds from envmap= / envmap_gain= (src/cmd/cmd.cpp:59-65):
+ * sets (or replaces) the environment looked up on a miss. rgb holds
+ * width*height linear RGB floats, row 0 at v = 1. width = 0 removes it. */
+int nr_scene_set_env(nr_scene* scene, int32_t width, int32_t height, const float* rgb, float gain);
 
 /* info[0..5] = triangles, materials, BVH nodes, BVH depth, emitters, device bytes. */
 int nr_scene_info(const nr_scene* scene, int64_t info[6]);

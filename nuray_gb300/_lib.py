@@ -59,6 +59,7 @@ SIGNATURES = {
     "nr_scene_create": [_vp, _vp],
     "nr_scene_load": [_cp, _vp],
     "nr_scene_destroy": [_vp],
+    "nr_scene_set_env": [_vp, _i32, _i32, _vp, ctypes.c_float],
     "nr_scene_info": [_vp, _vp],
     "nr_scene_export": [_vp, _vp, _vp, _vp, _vp, _vp],
     "nr_bvh_export": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
@@ -145,6 +146,14 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+    def set_env(self, rgb, gain=1.0):
+        """Attaches an environment map ((h, w, 3) float32, row 0 at v = 1); None removes it."""
+        if rgb is None:
+            check(lib().nr_scene_set_env(self._h, 0, 0, None, gain))
+            return
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        check(lib().nr_scene_set_env(self._h, rgb.shape[1], rgb.shape[0], _ptr(rgb), gain))
 
     def info(self):
         a = np.zeros(6, np.int64)

@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnuray_gpu.so")
+CLI = os.path.join(OUT, "nuray")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,15 +34,19 @@ def _run(cmd):
 
 
 def sources():
-    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cpp", ".h", ".cuh"))]
+    out = []
+    for d in (CSRC, os.path.join(CSRC, "cli")):
+        out += [os.path.join(d, f) for f in sorted(os.listdir(d)) if f.endswith((".cu", ".cpp", ".h", ".cuh"))]
+    return out
 
 
 def up_to_date():
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
-    deps = sources() + [os.path.join(HERE, "..", "include", "nuray.h"), os.path.abspath(__file__)]
-    return all(os.path.getmtime(p) <= t for p in deps)
+    deps = sources() + [os.path.join(HERE, "..", "include", h) for h in ("nuray.h", "nuray_renderer.hpp")]
+    deps.append(os.path.abspath(__file__))
+    return os.path.exists(CLI) and all(os.path.getmtime(p) <= t for p in deps)
 
 
 def build(force=False, verbose=False):
@@ -69,6 +74,9 @@ def build(force=False, verbose=False):
     tmp = LIB + ".tmp"
     _run([_nvcc(), *ARCH, "-shared", "-o", tmp, *[j[0] for j in jobs], "-lpthread"])
     os.replace(tmp, LIB)
+    # the command-line front end, linked against the library
+    _run(["g++", "-O2", "-std=c++17", *inc, os.path.join(CSRC, "cli", "nuray_main.cpp"), "-o", CLI,
+          "-L", OUT, "-lnuray_gpu", "-Wl,-rpath,$ORIGIN", "-lpthread"])
     return LIB
 
 

@@ -232,6 +232,7 @@ void upload_scene(nr_scene* s) {
     D.env_tex = H.env_tex;
     D.env_gain = H.env_gain;
     D.max_depth = B.max_depth;
+    D.num_nodes = ng;
     if (n == 0) {
         D.root_ref = INT32_MIN;
     } else {
@@ -358,8 +359,10 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         W.sample0 = (uint32_t)sample0;
         W.pix_xy = dev_pix;
         mark(-1);
-        nr::launch_reset_counters(s->ps.counters, st);
-        nr::launch_raygen(s->ps, W, A.cam, film_h, A.pol, st);
+        // queue_in / queue_out swap roles every bounce
+        nr::PathState P = s->ps;
+        nr::launch_reset_counters(P.counters, st);
+        nr::launch_raygen(P, W, A.cam, film_h, A.pol, st);
         S.kernel_launches += 2;
         mark(3);
         int live = W.count;
@@ -376,7 +379,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                 ev_kind.push_back(-1); ev_kind.push_back(0); ev_kind.push_back(1); ev_kind.push_back(2);
                 nev += 4;
             }
-            nr::launch_bounce(s->ps, s->dev, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count);
+            nr::launch_bounce(P, s->dev, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count);
+            std::swap(P.queue_in, P.queue_out);
             S.bounces++;
             S.trace_launches++;
             S.kernel_launches += 4;
@@ -420,7 +424,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         *dst[ev_kind[i]] += ms;
     }
     S.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (c[nr::CNT_ERR] != 0) throw NrError(NR_ERR_DEVICE, "traversal stack overflow in a kernel");
+    if (c[nr::CNT_ERR] != 0)
+        throw NrError(NR_ERR_DEVICE, "traversal error bits " + std::to_string(c[nr::CNT_ERR]) + " (1 stack overflow, 2 step cap)");
 }
 
 }  // namespace
@@ -460,6 +465,34 @@ int nr_scene_load(const char* text, nr_scene** out) {
 
 int nr_scene_destroy(nr_scene* s) {
     return guarded([&]() { delete s; });
+}
+
+int nr_scene_set_env(nr_scene* s, int32_t width, int32_t height, const float* rgb, float gain) {
+    return guarded([&]() {
+        if (!s || width < 0 || height < 0 || (width > 0 && (height == 0 || !rgb))) throw NrError(NR_ERR_INVALID, "bad argument");
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        nr::HostScene& H = s->host;
+        // drop a previously attached environment that no material uses
+        if (H.env_tex >= 0 && H.env_tex == (int)H.tex_wh.size() / 2 - 1) {
+            bool used = false;
+            for (const auto& m : H.mats) used = used || m.tex0 == H.env_tex || m.tex1 == H.env_tex;
+            if (!used) {
+                size_t texels = (size_t)H.tex_wh[2 * H.env_tex] * H.tex_wh[2 * H.env_tex + 1];
+                H.tex_data.resize(H.tex_data.size() - 3 * texels);
+                H.tex_wh.resize(H.tex_wh.size() - 2);
+            }
+        }
+        H.env_tex = -1;
+        if (width > 0) {
+            H.tex_wh.push_back(width);
+            H.tex_wh.push_back(height);
+            H.tex_data.insert(H.tex_data.end(), rgb, rgb + 3 * (size_t)width * height);
+            H.env_tex = (int)H.tex_wh.size() / 2 - 1;
+        }
+        H.env_gain = gain;
+        upload_scene(s);
+    });
 }
 
 int nr_scene_info(const nr_scene* s, int64_t info[6]) {
@@ -542,7 +575,7 @@ int nr_intersect(nr_scene* s, int32_t n, const float* o, const float* d, int32_t
         NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters + nr::CNT_ERR, 4, cudaMemcpyDeviceToHost, st));
         NR_CUDA(cudaStreamSynchronize(st));
         err = s->counters_host[0];
-        if (err) throw NrError(NR_ERR_DEVICE, "traversal stack overflow in a kernel");
+        if (err) throw NrError(NR_ERR_DEVICE, "traversal error bits " + std::to_string(err) + " (1 stack overflow, 2 step cap)");
     });
 }
 

@@ -190,7 +190,11 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
     int sp = 0;
     int ref = S.root_ref;
     uint32_t nv = 0, nt = 0;
+    // every node is entered at most once per ray; the cap only guards against
+    // a corrupted node array
+    int budget = 2 * S.num_nodes + 8;
     while (true) {
+        if (--budget < 0) { atomicOr(err, 2u); break; }
         if (ref >= 0) {
             const GpuNode& N = S.nodes[ref];
             float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
@@ -255,7 +259,9 @@ __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float 
     int sp = 0;
     int ref = S.root_ref;
     const float limit = fminf(1e18f, __uint_as_float(__float_as_uint(tmax) + 1u));  // accepts t <= tmax
+    int budget = 2 * S.num_nodes + 8;
     while (true) {
+        if (--budget < 0) { atomicOr(err, 2u); return false; }
         if (ref >= 0) {
             const GpuNode& N = S.nodes[ref];
             float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);

@@ -52,6 +52,7 @@ struct DeviceScene {
     int32_t env_tex;
     float env_gain;
     int32_t max_depth;        // deepest leaf (root = 0)
+    int32_t num_nodes;        // internal nodes
 };
 
 // Render policy decoded from the parameter string.
@@ -95,7 +96,7 @@ enum Counter {
     CNT_WORK = 3,      // persistent-kernel work cursor (closest hit)
     CNT_WORK_SH = 4,   // persistent-kernel work cursor (shadow)
     CNT_CAT = 8,       // 8..14: per-category counts
-    CNT_ERR = 16,      // internal error word (stack overflow etc.), 0 = fine
+    CNT_ERR = 16,      // internal error bits: 1 stack overflow, 2 traversal step cap; 0 = fine
     CNT_RAYS = 18,     // 64-bit totals (lo, hi): extension rays,
     CNT_SHRAYS = 20,   // shadow rays,
     CNT_NODES = 22,    // BVH nodes visited by closest-hit rays (instrumented runs),
