@@ -551,7 +551,7 @@ int nr_intersect(nr_scene* s, int32_t n, const float* o, const float* d, int32_t
         float *dT = t, *dB1 = b1, *dB2 = b2;
         if (!(flags & NR_PTR_DEVICE)) {
             size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4;
-            s->scratch.alloc(2 * f3 + 4 * f1 + 4 * 256);
+            s->scratch.alloc(2 * f3 + 4 * f1 + 6 * 256);  // six 256-byte aligned pieces
             char* p = s->scratch.as<char>();
             auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
             float* xo = (float*)take(f3);
@@ -656,7 +656,7 @@ int nr_material_probe(nr_scene* s, int32_t mat, int32_t n, const float* wo, cons
         NR_CUDA(cudaSetDevice(s->device));
         cudaStream_t st = s->stream;
         size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4, f4 = (size_t)n * 16;
-        s->scratch.alloc(4 * f3 + f4 + 2 * f3 + f1 + 16 * 256);
+        s->scratch.alloc(4 * f3 + f4 + 2 * f3 + f1 + 8 * 256);  // eight 256-byte aligned pieces
         char* p = s->scratch.as<char>();
         auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
         float *dwo = (float*)take(f3), *dn = (float*)take(f3), *dwi = (float*)take(f3), *duv = (float*)take(f3);
