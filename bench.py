@@ -42,6 +42,10 @@ MEASURED = os.path.join(ROOT, "MEASURED_PEAKS.json")
 BYTES_NODE = 64      # one internal node: both child boxes + references
 BYTES_TRI = 48       # one triangle: p0, e1, e2 (+ ids)
 BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry, material type
+# DRAM bytes (read + write) per closest-hit ray of k_trace, from one ncu
+# capture of a bounce-0 launch (profiles/k_trace_c2_first_bounce.md); the
+# roofline's `traffic` scales it to a full launch by rays per launch.
+TRACE_DRAM_BYTES_PER_RAY = 117.8
 
 
 def parse():
@@ -293,14 +297,9 @@ def main():
             "tris_per_ray": round(cnt["tris_tested"] / max(1, cnt["rays"]), 2),
             "avg_launch_ms": round(trace_ms / max(1, trace_launches), 4),
             "share_of_step": round(trace_ms / ms, 3)}
-    traffic_file = os.path.join(ROOT, "profiles", "k_trace_traffic.json")
-    if os.path.exists(traffic_file):
-        try:
-            tr = json.load(open(traffic_file))
-            roof["traffic"] = round(tr["dram_bytes_per_ray"] * rays / max(1, trace_launches))
-            roof["traffic_note"] = tr.get("note")
-        except Exception:
-            pass
+    roof["traffic"] = round(TRACE_DRAM_BYTES_PER_RAY * rays / max(1, trace_launches))
+    roof["traffic_note"] = ("ncu DRAM bytes per ray of a bounce-0 k_trace launch (small case of the same scene) "
+                            "x rays per launch")
 
     cpu = None
     if not args.no_cpu and world == 1:

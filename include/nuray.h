@@ -25,6 +25,8 @@
  *   nr_render_samples                the per-sample loop body of RendererPTLS::render
  *                                    (src/renderer/rendererptls.cpp:170-174) for listed pixels
  *   nr_material_probe                Material::bxdf/pdf/sampleBxdf (src/material/material.h:7-24)
+ *   nr_nrc_*                         NNNodeMultiLayerPerceptron::eval / train (src/nn/nnnode.cpp:175-201)
+ *   nr_scene_attach_nrc              RendererNRC's cache query (src/renderer/renderernrc.cpp:130-133)
  *   nr_get_stats / nr_scene_stream   no reference counterpart (the reference reports only a
  *                                    wall-clock "secs used", src/renderer/rendererptls.cpp:232-233)
  */
@@ -190,7 +192,7 @@ int nr_camera_from_params(const char* params, nr_camera* cam);
  * imgw imgh spp prr mis (reference keys and defaults) plus seed (Philox seed,
  * default 0), rrdepth (first vertex where Russian roulette applies, default 0
  * as in the reference), maxdepth (0 = unbounded as in the reference),
- * wave (paths per wavefront batch, default 2^21), sample0 (index of the first
+ * wave (paths per wavefront batch, default 2^23), sample0 (index of the first
  * sample, default 0: renders of disjoint sample ranges are independent and
  * their films sum), profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
  * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
@@ -213,6 +215,41 @@ int nr_get_stats(const nr_scene* scene, nr_stats* stats);
 /* The CUDA stream (cudaStream_t) on which the scene's kernels run, for
  * callers that time or order work against it. */
 int nr_scene_stream(const nr_scene* scene, void** stream);
+
+/* ------------------------------------------------------------------------
+ * Neural radiance cache. Replaces the reference's nrc renderer network
+ * (NNNodeMultiLayerPerceptron::eval / train, src/nn/nnnode.h:64-85,
+ * src/nn/nnnode.cpp:175-201) with a fused 80-64-64-64-64-3 ReLU MLP on the
+ * BF16 tensor cores with FP32 accumulation, FP32 master weights and Adam.
+ * Loss: mean over rows and channels of (o - y)^2 / (o^2 + 0.01), the
+ * reference's relative L2 (src/nn/nnnode.cpp:187-201) with o held constant
+ * in the denominator.
+ * ------------------------------------------------------------------------ */
+#define NR_NRC_INPUTS 80
+
+typedef struct nr_nrc nr_nrc;
+
+/* params: lr (1e-3), beta1 (0.9), beta2 (0.99), eps (1e-8), seed (0, for the
+ * Glorot-uniform initialisation). Allocates on the current device. */
+int nr_nrc_create(const char* params, nr_nrc** out);
+int nr_nrc_destroy(nr_nrc* nrc);
+/* Number of FP32 parameters (weights and biases, layout in nrc.h). */
+int nr_nrc_num_params(int64_t* n);
+int nr_nrc_get_params(nr_nrc* nrc, float* params);
+int nr_nrc_set_params(nr_nrc* nrc, const float* params);
+/* Forward pass for n rows of NR_NRC_INPUTS floats (rounded to BF16); out n*3. */
+int nr_nrc_infer(nr_nrc* nrc, int32_t n, const float* x, float* out);
+/* Gradient of the loss over n rows (no update): grad receives
+ * nr_nrc_num_params floats; loss the mean loss. */
+int nr_nrc_gradient(nr_nrc* nrc, int32_t n, const float* x, const float* y, float* grad, float* loss);
+/* One Adam step on the loss over n rows; loss (may be NULL) receives the
+ * mean loss before the step. */
+int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, float* loss);
+/* Attaches a cache to a scene: nr_render with nrc=1 then ends non-training
+ * paths at the vertex after their first diffuse bounce with the cache's
+ * prediction and trains the cache online on the suffix radiance of
+ * nrc_train (default 16384) training paths per wavefront batch. NULL detaches. */
+int nr_scene_attach_nrc(nr_scene* scene, nr_nrc* nrc);
 
 /* Material::bxdf, ::pdf and ::sampleBxdf of scene material `mat` evaluated
  * on the device for n queries: wo, nrm, wi, uv (3 floats each) and 4

@@ -16,6 +16,8 @@
 #include "../../include/nuray.h"
 #include "host_scene.h"
 #include "integrator.h"
+#include "nrc.h"
+#include <random>
 
 namespace {
 
@@ -71,6 +73,34 @@ struct DevBuf {
 
 }  // namespace
 
+// One neural radiance cache on one device.
+struct nr_nrc {
+    std::mutex mu;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf pbuf;  // params | grad | m | v (FP32) then the BF16 copy
+    nr::NrcDev dev{};
+    float lr = 1e-3f, b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+    int step = 0;
+    // scratch for batches: x (BF16), y, out, acts, dz, loss
+    DevBuf batch;
+    int batch_cap = 0;
+    __nv_bfloat16 *x = nullptr, *acts = nullptr, *dz = nullptr;
+    float *y = nullptr, *out = nullptr, *loss = nullptr;
+    float* xf = nullptr;  // FP32 staging of caller inputs
+    float* loss_host = nullptr;  // pinned
+
+    ~nr_nrc() {
+        cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        pbuf.release();
+        batch.release();
+        if (loss_host) cudaFreeHost(loss_host);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
 struct nr_scene {
     std::mutex mu;
     int device = 0;
@@ -88,12 +118,18 @@ struct nr_scene {
     uint32_t* counters_host = nullptr;  // pinned
     nr_stats stats{};
     std::vector<cudaEvent_t> ev_pool;  // profile=1: events around every kernel group
+    nr_nrc* nrc = nullptr;             // attached cache (not owned)
+    DevBuf nrc_mem;                    // query / training records of the online cache
+    int nrc_cap = 0, nrc_tcap = 0;
+    nr::NrcCtx nrc_ctx{};
+    float* nrc_pred = nullptr;
+    float nrc_last_loss = 0.f;
 
     ~nr_scene() {
         if (device >= 0) cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
         for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &path_mem, &film,
-                        &out_hdr, &out_rgb8, &pix_list, &scratch})
+                        &out_hdr, &out_rgb8, &pix_list, &scratch, &nrc_mem})
             b->release();
         if (counters_host) cudaFreeHost(counters_host);
         for (auto& e : ev_pool) cudaEventDestroy(e);
@@ -282,6 +318,39 @@ void ensure_paths(nr_scene* s, int cap) {
     s->capacity = cap;
 }
 
+// Sizes the batch scratch of a cache for m rows.
+void nrc_ensure_batch(nr_nrc* c, int m) {
+    if (m <= c->batch_cap) return;
+    size_t M = (size_t)m;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t bytes = al(M * NRC_IN * 2) + al(M * 12) + al(M * 12) + al(4 * M * NRC_H * 2) + al(5 * M * NRC_H * 2) + 256 +
+                   al(M * NRC_IN * 4);
+    c->batch.alloc(bytes);
+    char* p = c->batch.as<char>();
+    auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
+    c->x = (__nv_bfloat16*)take(M * NRC_IN * 2);
+    c->y = (float*)take(M * 12);
+    c->out = (float*)take(M * 12);
+    c->acts = (__nv_bfloat16*)take(4 * M * NRC_H * 2);
+    c->dz = (__nv_bfloat16*)take(5 * M * NRC_H * 2);
+    c->loss = (float*)take(4);
+    c->xf = (float*)take(M * NRC_IN * 4);
+    c->batch_cap = m;
+}
+
+// Gradient (and, when `update`, one Adam step) on m rows already on the
+// device: x BF16 [m][80], y [m][3]. Returns the summed loss asynchronously in c->loss.
+void nrc_train_device(nr_nrc* c, const __nv_bfloat16* x, const float* y, int m, bool update, cudaStream_t st) {
+    nrc_ensure_batch(c, m);
+    NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
+    nr::nrc_launch_forward(c->dev, x, m, c->out, c->acts, c->num_sms, st);
+    nr::nrc_launch_backward(c->dev, x, c->out, y, c->acts, c->dz, m, c->loss, c->num_sms, st);
+    if (update) {
+        c->step++;
+        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, st);
+    }
+}
+
 struct RenderArgs {
     nr::Policy pol;
     nr_camera cam;
@@ -290,6 +359,11 @@ struct RenderArgs {
     bool profile;
     bool count;
     int sample0;
+    bool nrc;
+    int nrc_train;    // training paths per wavefront batch
+    int nrc_steps;    // Adam steps per batch
+    int nrc_query;    // 0: train only
+    float nrc_rough;  // roughness from which a GGX vertex is diffuse
 };
 
 RenderArgs parse_args(const nr_camera* cam, const char* params) {
@@ -307,10 +381,16 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgw = c.get_int("imgw", 1);
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
-    a.wave = c.get_int("wave", 1 << 21);
+    a.wave = c.get_int("wave", 1 << 23);
     a.profile = c.get_int("profile", 0) != 0;
     a.count = c.get_int("count", 0) != 0;
     a.sample0 = c.get_int("sample0", 0);
+    a.nrc = c.get_int("nrc", 0) != 0;
+    a.nrc_train = c.get_int("nrc_train", 16384);
+    a.nrc_steps = c.get_int("nrc_steps", 4);
+    a.nrc_query = c.get_int("nrc_query", 1);
+    a.nrc_rough = c.get_float("nrc_rough", 0.2f);
+    if (a.nrc && (a.nrc_train <= 0 || a.nrc_steps <= 0)) throw NrError(NR_ERR_INVALID, "nrc_train and nrc_steps must be positive");
     if (a.sample0 < 0) throw NrError(NR_ERR_INVALID, "sample0 must be >= 0");
     if (a.pol.imgw <= 0 || a.pol.imgh <= 0) throw NrError(NR_ERR_INVALID, "imgw and imgh must be positive");
     if ((int64_t)a.pol.imgw * a.pol.imgh > (1LL << 30)) throw NrError(NR_ERR_INVALID, "image too large");
@@ -330,6 +410,43 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     const int cap = (int)std::min<uint64_t>(total, (uint64_t)A.wave);
     ensure_paths(s, cap);
     cudaStream_t st = s->stream;
+    const bool use_nrc = A.nrc;
+    if (use_nrc) {
+        if (!s->nrc) throw NrError(NR_ERR_INVALID, "nrc=1 needs a cache attached with nr_scene_attach_nrc");
+        const int depth_cap = A.pol.maxdepth > 0 ? A.pol.maxdepth : 16;
+        const int tcap = A.nrc_train * depth_cap;
+        if (cap > s->nrc_cap || tcap > s->nrc_tcap) {
+            auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+            size_t C = (size_t)cap, T = (size_t)tcap;
+            s->nrc_mem.alloc(al(C * NRC_IN * 2) + al(C * 4) + al(C * 16) + al(T * NRC_IN * 2) + al(T * 4) + al(T * 16) * 2 +
+                             256 + al(C * 12));
+            char* p = s->nrc_mem.as<char>();
+            auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
+            nr::NrcCtx& X = s->nrc_ctx;
+            X.q_x = take(C * NRC_IN * 2);
+            X.q_slot = (int32_t*)take(C * 4);
+            X.q_thr = (float4*)take(C * 16);
+            X.t_x = take(T * NRC_IN * 2);
+            X.t_slot = (int32_t*)take(T * 4);
+            X.t_thr = (float4*)take(T * 16);
+            X.t_before = (float4*)take(T * 16);
+            X.counters = (uint32_t*)take(16);
+            s->nrc_pred = (float*)take(C * 12);
+            s->nrc_cap = cap;
+            s->nrc_tcap = tcap;
+        }
+        nr::NrcCtx& X = s->nrc_ctx;
+        X.tcap = s->nrc_tcap;
+        X.train_stride = (uint32_t)std::max<int64_t>(1, (int64_t)cap / A.nrc_train);
+        X.query = A.nrc_query;
+        X.rough = A.nrc_rough;
+        for (int k = 0; k < 3; ++k) {
+            float ext = s->dev.root_hi[k] - s->dev.root_lo[k];
+            X.lo[k] = s->dev.root_lo[k];
+            X.inv_ext[k] = ext > 0.f ? 1.0f / ext : 0.f;
+        }
+        nrc_ensure_batch(s->nrc, std::max(s->nrc_tcap, cap));
+    }
     const float film_h = nr::film_height(A.cam);
     auto t0 = std::chrono::steady_clock::now();
     nr_stats& S = s->stats;
@@ -362,6 +479,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         // queue_in / queue_out swap roles every bounce
         nr::PathState P = s->ps;
         nr::launch_reset_counters(P.counters, st);
+        if (use_nrc) NR_CUDA(cudaMemsetAsync(s->nrc_ctx.counters, 0, 8, st));
         nr::launch_raygen(P, W, A.cam, film_h, A.pol, st);
         S.kernel_launches += 2;
         mark(3);
@@ -379,7 +497,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                 ev_kind.push_back(-1); ev_kind.push_back(0); ev_kind.push_back(1); ev_kind.push_back(2);
                 nev += 4;
             }
-            nr::launch_bounce(P, s->dev, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count);
+            nr::launch_bounce(P, s->dev, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count,
+                              use_nrc ? &s->nrc_ctx : nullptr);
             std::swap(P.queue_in, P.queue_out);
             S.bounces++;
             S.trace_launches++;
@@ -391,6 +510,43 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                 NR_CUDA(cudaStreamSynchronize(st));
                 live = (int)s->counters_host[nr::CNT_IN];
                 if (live == 0) break;
+            }
+        }
+        if (use_nrc) {
+            // cache queries of this batch, then training on its training paths
+            uint32_t qt[2];
+            NR_CUDA(cudaMemcpyAsync(s->counters_host, s->nrc_ctx.counters, 8, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+            qt[0] = s->counters_host[0];
+            qt[1] = std::min<uint32_t>(s->counters_host[1], (uint32_t)s->nrc_tcap);
+            nr_nrc* c = s->nrc;
+            if (qt[0] > 0) {
+                nr::nrc_launch_forward(c->dev, (const __nv_bfloat16*)s->nrc_ctx.q_x, (int)qt[0], s->nrc_pred, nullptr,
+                                       c->num_sms, st);
+                nr::launch_nrc_apply(s->ps, s->nrc_ctx, s->nrc_pred, (int)qt[0], st);
+                S.kernel_launches += 2;
+            }
+            if (qt[1] > 0) {
+                nr::launch_nrc_targets(s->ps, s->nrc_ctx, c->y, (int)qt[1], 1e3f, st);
+                const int steps = std::min<int>(A.nrc_steps, (int)qt[1]);
+                const int chunk = ((int)qt[1] + steps - 1) / steps;
+                for (int k = 0; k < steps; ++k) {
+                    int m0 = k * chunk, m = std::min<int>(chunk, (int)qt[1] - m0);
+                    if (m <= 0) break;
+                    const __nv_bfloat16* x = (const __nv_bfloat16*)s->nrc_ctx.t_x + (size_t)m0 * NRC_IN;
+                    // y of the chunk lives at c->y + 3 m0; the batch scratch is sized for all records
+                    nr::nrc_launch_forward(c->dev, x, m, c->out, c->acts, c->num_sms, st);
+                    NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
+                    nr::nrc_launch_backward(c->dev, x, c->out, c->y + 3 * (size_t)m0, c->acts, c->dz, m, c->loss,
+                                            c->num_sms, st);
+                    c->step++;
+                    nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, st);
+                    S.kernel_launches += 9;
+                }
+                NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, st));
+                NR_CUDA(cudaStreamSynchronize(st));
+                s->nrc_last_loss = *c->loss_host / (3.0f * (float)chunk);
+                S.kernel_launches += 1;
             }
         }
         mark(-1);
@@ -637,6 +793,149 @@ int nr_get_stats(const nr_scene* s, nr_stats* st) {
     return guarded([&]() {
         if (!s || !st) throw NrError(NR_ERR_INVALID, "null argument");
         *st = s->stats;
+    });
+}
+
+// ------------------------------------------------------------------ neural radiance cache
+int nr_nrc_num_params(int64_t* n) {
+    return guarded([&]() {
+        if (!n) throw NrError(NR_ERR_INVALID, "null argument");
+        *n = NRC_NUM_PARAMS;
+    });
+}
+
+int nr_nrc_create(const char* params, nr_nrc** out) {
+    return guarded([&]() {
+        if (!out) throw NrError(NR_ERR_INVALID, "null argument");
+        *out = nullptr;
+        nr::Config c(params);
+        auto n = std::make_unique<nr_nrc>();
+        NR_CUDA(cudaGetDevice(&n->device));
+        NR_CUDA(cudaDeviceGetAttribute(&n->num_sms, cudaDevAttrMultiProcessorCount, n->device));
+        NR_CUDA(cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking));
+        NR_CUDA(cudaMallocHost(&n->loss_host, 4));
+        n->lr = c.get_float("lr", 1e-3f);
+        n->b1 = c.get_float("beta1", 0.9f);
+        n->b2 = c.get_float("beta2", 0.99f);
+        n->eps = c.get_float("eps", 1e-8f);
+        nr::nrc_setup();
+        const size_t P = NRC_NUM_PARAMS;
+        n->pbuf.alloc(4 * P * 4 + P * 2 + 256);
+        float* f = n->pbuf.as<float>();
+        n->dev.params = f;
+        n->dev.grad = f + P;
+        n->dev.m = f + 2 * P;
+        n->dev.v = f + 3 * P;
+        n->dev.wb = reinterpret_cast<__nv_bfloat16*>(f + 4 * P);
+        // Glorot-uniform weights, zero biases; output rows 3..7 stay zero
+        std::vector<float> init(P, 0.0f);
+        std::mt19937_64 rng((uint64_t)c.get_int("seed", 0));
+        auto fill = [&](int off, int rows, int cols, int used_rows) {
+            float a = std::sqrt(6.0f / (float)(cols + used_rows));
+            std::uniform_real_distribution<float> U(-a, a);
+            for (int r = 0; r < used_rows; ++r)
+                for (int k = 0; k < cols; ++k) init[off + r * cols + k] = U(rng);
+            (void)rows;
+        };
+        fill(NRC_OFF_W0, NRC_H, NRC_IN, NRC_H);
+        fill(NRC_OFF_W1, NRC_H, NRC_H, NRC_H);
+        fill(NRC_OFF_W2, NRC_H, NRC_H, NRC_H);
+        fill(NRC_OFF_W3, NRC_H, NRC_H, NRC_H);
+        fill(NRC_OFF_W4, NRC_OUT_PAD, NRC_H, NRC_OUT);
+        NR_CUDA(cudaMemcpyAsync(n->dev.params, init.data(), P * 4, cudaMemcpyHostToDevice, n->stream));
+        NR_CUDA(cudaMemsetAsync(n->dev.grad, 0, 3 * P * 4, n->stream));
+        nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb, P, n->stream);
+        NR_CUDA(cudaStreamSynchronize(n->stream));
+        *out = n.release();
+    });
+}
+
+int nr_nrc_destroy(nr_nrc* n) {
+    return guarded([&]() { delete n; });
+}
+
+int nr_nrc_get_params(nr_nrc* n, float* out) {
+    return guarded([&]() {
+        if (!n || !out) throw NrError(NR_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(n->mu);
+        NR_CUDA(cudaSetDevice(n->device));
+        NR_CUDA(cudaMemcpyAsync(out, n->dev.params, NRC_NUM_PARAMS * 4, cudaMemcpyDeviceToHost, n->stream));
+        NR_CUDA(cudaStreamSynchronize(n->stream));
+    });
+}
+
+int nr_nrc_set_params(nr_nrc* n, const float* in) {
+    return guarded([&]() {
+        if (!n || !in) throw NrError(NR_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(n->mu);
+        NR_CUDA(cudaSetDevice(n->device));
+        NR_CUDA(cudaMemcpyAsync(n->dev.params, in, NRC_NUM_PARAMS * 4, cudaMemcpyHostToDevice, n->stream));
+        NR_CUDA(cudaMemsetAsync(n->dev.grad, 0, 3 * (size_t)NRC_NUM_PARAMS * 4, n->stream));
+        nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb, NRC_NUM_PARAMS, n->stream);
+        n->step = 0;
+        NR_CUDA(cudaStreamSynchronize(n->stream));
+    });
+}
+
+namespace {
+// Uploads n rows of FP32 inputs and converts them to BF16 in the batch scratch.
+void nrc_upload_x(nr_nrc* c, int n, const float* x) {
+    nrc_ensure_batch(c, n);
+    NR_CUDA(cudaMemcpyAsync(c->xf, x, (size_t)n * NRC_IN * 4, cudaMemcpyHostToDevice, c->stream));
+    nr::nrc_launch_to_bf16(c->xf, c->x, (size_t)n * NRC_IN, c->stream);
+}
+}  // namespace
+
+int nr_nrc_infer(nr_nrc* c, int32_t n, const float* x, float* out) {
+    return guarded([&]() {
+        if (!c || n < 0 || (n > 0 && (!x || !out))) throw NrError(NR_ERR_INVALID, "bad argument");
+        if (n == 0) return;
+        std::lock_guard<std::mutex> lk(c->mu);
+        NR_CUDA(cudaSetDevice(c->device));
+        nrc_upload_x(c, n, x);
+        nr::nrc_launch_forward(c->dev, c->x, n, c->out, nullptr, c->num_sms, c->stream);
+        NR_CUDA(cudaMemcpyAsync(out, c->out, (size_t)n * 12, cudaMemcpyDeviceToHost, c->stream));
+        NR_CUDA(cudaStreamSynchronize(c->stream));
+        NR_CUDA(cudaGetLastError());
+    });
+}
+
+static int nrc_grad_impl(nr_nrc* c, int32_t n, const float* x, const float* y, float* grad, float* loss, bool update) {
+    return guarded([&]() {
+        if (!c || n <= 0 || !x || !y) throw NrError(NR_ERR_INVALID, "bad argument");
+        std::lock_guard<std::mutex> lk(c->mu);
+        NR_CUDA(cudaSetDevice(c->device));
+        nrc_upload_x(c, n, x);
+        NR_CUDA(cudaMemcpyAsync(c->y, y, (size_t)n * 12, cudaMemcpyHostToDevice, c->stream));
+        nrc_train_device(c, c->x, c->y, n, false, c->stream);
+        if (grad) NR_CUDA(cudaMemcpyAsync(grad, c->dev.grad, NRC_NUM_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream));
+        if (update) {
+            c->step++;
+            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->stream);
+        } else {
+            NR_CUDA(cudaMemsetAsync(c->dev.grad, 0, NRC_NUM_PARAMS * 4, c->stream));
+        }
+        NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, c->stream));
+        NR_CUDA(cudaStreamSynchronize(c->stream));
+        NR_CUDA(cudaGetLastError());
+        if (loss) *loss = *c->loss_host / (3.0f * (float)n);
+    });
+}
+
+int nr_nrc_gradient(nr_nrc* c, int32_t n, const float* x, const float* y, float* grad, float* loss) {
+    return nrc_grad_impl(c, n, x, y, grad, loss, false);
+}
+
+int nr_nrc_train_step(nr_nrc* c, int32_t n, const float* x, const float* y, float* loss) {
+    return nrc_grad_impl(c, n, x, y, nullptr, loss, true);
+}
+
+int nr_scene_attach_nrc(nr_scene* s, nr_nrc* c) {
+    return guarded([&]() {
+        if (!s) throw NrError(NR_ERR_INVALID, "null scene");
+        if (c && c->device != s->device) throw NrError(NR_ERR_INVALID, "cache and scene live on different devices");
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->nrc = c;
     });
 }
 

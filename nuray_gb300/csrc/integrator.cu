@@ -112,7 +112,18 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
 }
 
 // ---------------------------------------------------------------- shading
-__device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot) {
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+// Training paths of the online cache: a fixed hash of (pixel, sample).
+__device__ __forceinline__ bool nrc_is_training(uint32_t pixel, uint32_t sample, uint32_t stride) {
+    return hash32(pixel ^ hash32(sample + 0x9e3779b9u)) % stride == 0u;
+}
+
+template <bool NRC>
+__device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
+                                          const NrcCtx& C) {
     float4 h = P.hit[slot];
     float4 thr = P.thr[slot];
     uint4 meta = P.meta[slot];
@@ -153,7 +164,31 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     Stream rng;
     rng.init(pol.seed_lo, pol.seed_hi, meta.x, meta.y, meta.z);
     float fac = 1.0f;
-    const int depth = (int)meta.w;
+    const int depth = (int)(meta.w & NR_META_DEPTH_MASK);
+    uint32_t flags = meta.w & NR_META_SEEN_DIFFUSE;
+    if (NRC) {
+        const bool train = nrc_is_training(meta.x, meta.y, C.train_stride);
+        if (!train && flags && C.query) {
+            // past the first diffuse bounce: the cache stands in for the rest of the path
+            int q = warp_append(true, &C.counters[0]);
+            C.q_slot[q] = slot;
+            C.q_thr[q] = make_float4(T.x, T.y, T.z, 0.f);
+            nrc_encode(reinterpret_cast<uint32_t*>(C.q_x) + (size_t)q * 40, C.lo, C.inv_ext, hit_pos, wo, normal,
+                       nrc_roughness(M), M.c0);
+            return;
+        }
+        if (train) {
+            int r = warp_append(true, &C.counters[1]);
+            if (r < C.tcap) {
+                C.t_slot[r] = slot;
+                C.t_thr[r] = make_float4(T.x, T.y, T.z, 0.f);
+                C.t_before[r] = P.rad[slot];
+                nrc_encode(reinterpret_cast<uint32_t*>(C.t_x) + (size_t)r * 40, C.lo, C.inv_ext, hit_pos, wo, normal,
+                           nrc_roughness(M), M.c0);
+            }
+        }
+        if (nrc_diffuse(M, C.rough)) flags = NR_META_SEEN_DIFFUSE;
+    }
 
     // next-event estimation (rendererptls.cpp:49-78)
     if (mat_nee(type) && S.num_lights > 0) {
@@ -222,12 +257,13 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
     P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
     P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
-    P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, meta.w + 1u);
+    P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, (uint32_t)(depth + 1) | flags);
 }
 
 // Shades the bucketed queue: categories are contiguous, so each warp mostly
 // runs one material's code.
-__global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Policy pol, int capacity) {
+template <bool NRC>
+__global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Policy pol, int capacity, NrcCtx C) {
     uint32_t cnt[NUM_CAT], start[NUM_CAT];
     uint32_t total = 0;
 #pragma unroll
@@ -237,7 +273,7 @@ __global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Polic
 #pragma unroll
         for (int k = 1; k < NUM_CAT; ++k) if (i >= start[k]) c = k;
         int slot = P.sorted[(size_t)c * capacity + (i - start[c])];
-        shade_one(P, S, pol, slot);
+        shade_one<NRC>(P, S, pol, slot, C);
     }
 }
 
@@ -340,6 +376,34 @@ __global__ void k_finish(const float4* film, int npix, float inv_spp, float* hdr
     }
 }
 
+// ---------------------------------------------------------------- online cache
+// Adds the cache prediction of each query: L += T * max(0, nrc(x)).
+__global__ void k_nrc_apply(PathState P, NrcCtx C, const float* __restrict__ pred, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int slot = C.q_slot[i];
+    float4 t = C.q_thr[i], r = P.rad[slot];
+    const float* o = pred + 3 * (size_t)i;
+    P.rad[slot] = make_float4(r.x + t.x * fmaxf(0.f, o[0]), r.y + t.y * fmaxf(0.f, o[1]), r.z + t.z * fmaxf(0.f, o[2]), 0.f);
+}
+
+// Training targets: radiance the path gathered from the vertex on, divided by
+// the throughput that reached the vertex; channels with negligible
+// throughput copy the luminance-weighted value, and targets are clamped.
+__global__ void k_nrc_targets(PathState P, NrcCtx C, float* __restrict__ y, int n, float clamp_max) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int slot = C.t_slot[i];
+    float4 a = P.rad[slot], b = C.t_before[i], t = C.t_thr[i];
+    float d[3] = {a.x - b.x, a.y - b.y, a.z - b.z}, tt[3] = {t.x, t.y, t.z};
+    float tsum = tt[0] + tt[1] + tt[2], dsum = d[0] + d[1] + d[2];
+    for (int k = 0; k < 3; ++k) {
+        float v = tt[k] > 1e-4f ? d[k] / tt[k] : (tsum > 1e-4f ? dsum / tsum : 0.f);
+        if (!(v >= 0.f)) v = 0.f;  // NaN or negative
+        y[3 * (size_t)i + k] = fminf(v, clamp_max);
+    }
+}
+
 // ---------------------------------------------------------------- single queries
 __global__ void k_intersect(DeviceScene S, int n, const float* o, const float* d, int* tri, float* t, float* b1,
                             float* b2, uint32_t* err) {
@@ -389,14 +453,15 @@ void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, 
 }
 
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
-                   cudaStream_t st, cudaEvent_t* ev, bool count) {
+                   cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc) {
     if (ev) cudaEventRecord(ev[0], st);
     if (count) k_trace<true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
     else k_trace<false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
     if (ev) cudaEventRecord(ev[1], st);
     int shade_blocks = (max_count + 127) / 128;
     if (shade_blocks < 1) shade_blocks = 1;
-    k_shade<<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity);
+    if (nrc) k_shade<true><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, *nrc);
+    else k_shade<false><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, NrcCtx{});
     if (ev) cudaEventRecord(ev[2], st);
     if (count) k_shadow<true><<<g_shadow_blocks, 128, 0, st>>>(P, S);
     else k_shadow<false><<<g_shadow_blocks, 128, 0, st>>>(P, S);
@@ -405,6 +470,13 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
 }
 
 void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, 32, 0, st>>>(counters); }
+
+void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int n, cudaStream_t st) {
+    if (n > 0) k_nrc_apply<<<(n + 255) / 256, 256, 0, st>>>(P, C, pred, n);
+}
+void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, int n, float clamp_max, cudaStream_t st) {
+    if (n > 0) k_nrc_targets<<<(n + 255) / 256, 256, 0, st>>>(P, C, y, n, clamp_max);
+}
 
 void launch_film(const PathState& P, const WaveDesc& W, float4* film, cudaStream_t st) {
     k_film<<<(W.npix + 255) / 256, 256, 0, st>>>(P, W, film);

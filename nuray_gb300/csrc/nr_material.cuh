@@ -3,6 +3,8 @@
 // reference evaluates some sub-expressions in double through C++ promotion
 // (double literals, C libm calls on floats), which these restate in float.
 #pragma once
+#include <cuda_bf16.h>
+
 #include "nr_device.cuh"
 
 namespace nr {
@@ -268,6 +270,49 @@ __device__ __forceinline__ f3 mat_sample(const MatView& M, RNG& s, f3 wo, f3 n) 
         default:
             return mk(0.f);
     }
+}
+
+// Cache input encoding, 80 values: position in the scene box with 12
+// frequencies of sin/cos per axis (72), outgoing direction and shading
+// normal as (phi / 2pi + 0.5, theta / pi) (4), roughness (1), albedo (3).
+__device__ __forceinline__ float nrc_roughness(const MatView& M) {
+    if (M.type == NR_MAT_GGXR || M.type == NR_MAT_GGX) return M.alpha;
+    if (M.type == NR_MAT_GLASS) return 0.f;
+    return 1.f;
+}
+__device__ __forceinline__ bool nrc_diffuse(const MatView& M, float rough_min) {
+    if (M.type == NR_MAT_LAMBERT || M.type == NR_MAT_BLINNPHONG) return true;
+    if (M.type == NR_MAT_GGXR || M.type == NR_MAT_GGX) return M.alpha >= rough_min;
+    return false;
+}
+__device__ __forceinline__ void nrc_encode(uint32_t* dst, const float lo[3], const float inv_ext[3], f3 p, f3 wo, f3 n,
+                                           float rough, f3 albedo) {
+    float pp[3] = {(p.x - lo[0]) * inv_ext[0], (p.y - lo[1]) * inv_ext[1], (p.z - lo[2]) * inv_ext[2]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float f = 1.f;
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+            float sv, cv;
+            sincospif(pp[a] * f, &sv, &cv);
+            __nv_bfloat162 v = __floats2bfloat162_rn(sv, cv);
+            dst[a * 12 + k] = *reinterpret_cast<uint32_t*>(&v);
+            f *= 2.f;
+        }
+    }
+    auto sph = [](f3 d, float& u, float& v) {
+        u = atan2f(d.z, d.x) * (0.5f / 3.14159265f) + 0.5f;
+        v = acosf(fminf(1.f, fmaxf(-1.f, d.y))) * (1.f / 3.14159265f);
+    };
+    float u0, v0, u1, v1;
+    sph(wo, u0, v0);
+    sph(n, u1, v1);
+    __nv_bfloat162 e0 = __floats2bfloat162_rn(u0, v0), e1 = __floats2bfloat162_rn(u1, v1);
+    __nv_bfloat162 e2 = __floats2bfloat162_rn(rough, albedo.x), e3 = __floats2bfloat162_rn(albedo.y, albedo.z);
+    dst[36] = *reinterpret_cast<uint32_t*>(&e0);
+    dst[37] = *reinterpret_cast<uint32_t*>(&e1);
+    dst[38] = *reinterpret_cast<uint32_t*>(&e2);
+    dst[39] = *reinterpret_cast<uint32_t*>(&e3);
 }
 
 // Camera::generateRay (src/scene/camera.cpp:24-32); film_h precomputed as

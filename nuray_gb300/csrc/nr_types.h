@@ -85,6 +85,29 @@ struct PathState {
     uint32_t* counters;
 };
 
+// Online neural radiance cache inside the wavefront (k_shade<true>): query
+// and training records written during shading, consumed after the batch.
+struct NrcCtx {
+    void* q_x;            // __nv_bfloat16 [cap][80] query encodings
+    int32_t* q_slot;
+    float4* q_thr;        // throughput at the query vertex
+    void* t_x;            // __nv_bfloat16 [tcap][80] training encodings
+    int32_t* t_slot;
+    float4* t_thr;        // throughput on arrival at the vertex
+    float4* t_before;     // path radiance before the vertex
+    uint32_t* counters;   // [0] queries, [1] training records
+    int32_t tcap;
+    uint32_t train_stride;  // one path in train_stride is a training path
+    int32_t query;          // 0: train only (every path runs to the end)
+    float rough;            // GGX roughness from which a vertex counts as diffuse
+    float lo[3], inv_ext[3];  // scene box for the position encoding
+};
+
+// meta.w: vertex depth in the low 16 bits; this flag once a diffuse vertex
+// has been passed (NRC mode).
+#define NR_META_SEEN_DIFFUSE 0x80000000u
+#define NR_META_DEPTH_MASK 0xffffu
+
 // Shading categories for the material sort: one per material type, then
 // rays that left the scene.
 enum { CAT_MISS = 6, NUM_CAT = 7 };
