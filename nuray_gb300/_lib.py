@@ -70,6 +70,15 @@ SIGNATURES = {
     "nr_get_stats": [_vp, _vp],
     "nr_material_probe": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "nr_scene_stream": [_vp, _vp],
+    "nr_nrc_create": [_cp, _vp],
+    "nr_nrc_destroy": [_vp],
+    "nr_nrc_num_params": [_vp],
+    "nr_nrc_get_params": [_vp, _vp],
+    "nr_nrc_set_params": [_vp, _vp],
+    "nr_nrc_infer": [_vp, _i32, _vp, _vp],
+    "nr_nrc_gradient": [_vp, _i32, _vp, _vp, _vp, _vp],
+    "nr_nrc_train_step": [_vp, _i32, _vp, _vp, _vp],
+    "nr_scene_attach_nrc": [_vp, _vp],
 }
 
 _lib = None

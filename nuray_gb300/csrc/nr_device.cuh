@@ -140,6 +140,24 @@ __device__ __forceinline__ bool box_test(const SlabRay& r, float lx, float hx, f
     return tin <= tout && tout >= 0.0f;
 }
 
+// The same decision from approximate quotients (b - o) * RN(1/d): each is
+// within 2^-22.4 of the exact quotient, and the sign is exact, so the result
+// can only differ from the exact test when the entry and exit distances lie
+// within that error of each other; those cases are recomputed exactly.
+__device__ __forceinline__ bool box_test_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                              float& t_entry) {
+    float x1 = __fmul_rn(__fsub_rn(lx, r.ox), r.rx), x2 = __fmul_rn(__fsub_rn(hx, r.ox), r.rx);
+    float y1 = __fmul_rn(__fsub_rn(ly, r.oy), r.ry), y2 = __fmul_rn(__fsub_rn(hy, r.oy), r.ry);
+    float z1 = __fmul_rn(__fsub_rn(lz, r.oz), r.rz), z2 = __fmul_rn(__fsub_rn(hz, r.oz), r.rz);
+    float tin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fmaxf(fminf(z1, z2), -1e18f));
+    float tout = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fminf(fmaxf(z1, z2), 1e18f));
+    float margin = 1e-6f * fmaxf(fabsf(tin), fabsf(tout));  // about 8x the quotient error
+    if (tout < 0.0f) return false;  // exact: the signs of the quotients are exact
+    if (tin + margin < tout) { t_entry = tin; return true; }
+    if (tin > tout + margin) return false;
+    return box_test(r, lx, hx, ly, hy, lz, hz, t_entry);
+}
+
 // Triangle::intersection (src/scene/triangle.cpp:27-33) followed by the leaf
 // acceptance test of BVHNode::getIntersection (src/hierarchy/bvhnode.cpp:55-63):
 // t < limit && t > 0 && b1 >= 0 && b2 >= 0 && b1 + b2 <= 1.
@@ -158,6 +176,41 @@ __device__ __forceinline__ bool tri_test(f3 o, f3 d, float4 g0, float4 g1, float
     if (!(t < limit && t > 0.0f)) return false;
     b1 = qdiv(rdot(s1, s), q, rq);
     b2 = qdiv(rdot(s2, d), q, rq);
+    return b1 >= 0.0f && b2 >= 0.0f && __fadd_rn(b1, b2) <= 1.0f;
+}
+
+// tri_test with an approximate reciprocal of q: the decision is taken from
+// quotients within 2^-21 of the exact ones when every comparison clears that
+// margin, and recomputed with the exact division otherwise, so the accepted
+// set and the returned t, b1, b2 equal tri_test's.
+__device__ __forceinline__ bool tri_test_fast(f3 o, f3 d, float4 g0, float4 g1, float4 g2, float limit, float& t,
+                                              float& b1, float& b2) {
+    f3 p0 = xyz(g0), e1 = xyz(g1), e2 = xyz(g2);
+    f3 s = rsub3(o, p0);
+    f3 s1 = rcross(d, e2);
+    float q = add_1e6(rdot(s1, e1));
+    f3 s2 = rcross(s, e1);
+    float tt = rdot(s2, e2);
+    // t = tt / q > 0 needs equal signs and tt != 0 (exact)
+    if (tt == 0.0f || ((__float_as_uint(tt) ^ __float_as_uint(q)) & 0x80000000u)) return false;
+    float u = rdot(s1, s), v = rdot(s2, d);
+    // quotients from an approximate reciprocal (2 ulp): within 2^-21 of the exact ones
+    float rq = __fdividef(1.0f, q);
+    float ta = tt * rq, ua = u * rq, va = v * rq;
+    const float e = 1e-6f, tiny = 1e-30f;
+    if (ta > limit * (1.0f + e) || ua < -tiny || va < -tiny || ua + va > 1.0f + 2.0f * e) return false;
+    float rqe = __frcp_rn(q);
+    if (ta < limit * (1.0f - e) && ta > tiny && ua > tiny && va > tiny && ua + va < 1.0f - 2.0f * e) {
+        t = qdiv(tt, q, rqe);
+        b1 = qdiv(u, q, rqe);
+        b2 = qdiv(v, q, rqe);
+        return true;
+    }
+    // close to an edge, the far limit or zero: decide with the exact quotients
+    t = qdiv(tt, q, rqe);
+    if (!(t < limit && t > 0.0f)) return false;
+    b1 = qdiv(u, q, rqe);
+    b2 = qdiv(v, q, rqe);
     return b1 >= 0.0f && b2 >= 0.0f && __fadd_rn(b1, b2) <= 1.0f;
 }
 
@@ -201,8 +254,8 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
             int4 k = __ldg(&N.d);
             ++nv;
             float t0, t1;
-            bool h0 = box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
-            bool h1 = box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
+            bool h0 = box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
+            bool h1 = box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
             float lim = best_t * (1.0f + NR_PRUNE_MARGIN);
             h0 = h0 && t0 <= lim;
             h1 = h1 && t1 <= lim;
@@ -226,7 +279,7 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
                 float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
                 ++nt;
                 float t, u, v;
-                if (tri_test(o, d, g0, g1, g2, lt, t, u, v)) { lt = t; lb1 = u; lb2 = v; li = ti; }
+                if (tri_test_fast(o, d, g0, g1, g2, lt, t, u, v)) { lt = t; lb1 = u; lb2 = v; li = ti; }
             }
             if (li >= 0 && (lt < best_t || (lt == best_t && first > best_leaf))) {
                 best_t = lt; best_b1 = lb1; best_b2 = lb2; best = li; best_leaf = first;
@@ -268,8 +321,8 @@ __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float 
             int4 k = __ldg(&N.d);
             if (nodes_visited) ++*nodes_visited;
             float t0, t1;
-            bool h0 = box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) && t0 <= lim;
-            bool h1 = box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) && t1 <= lim;
+            bool h0 = box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) && t0 <= lim;
+            bool h1 = box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) && t1 <= lim;
             if (h0 && h1) {
                 int nr = k.x, fr = k.y;
                 if (t1 < t0) { nr = k.y; fr = k.x; }
@@ -287,7 +340,7 @@ __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float 
                 float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
                 if (tris_tested) ++*tris_tested;
                 float t, u, v;
-                if (tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
+                if (tri_test_fast(o, d, g0, g1, g2, limit, t, u, v)) return true;
             }
         }
         if (sp == 0) break;

@@ -1,0 +1,165 @@
+"""The cache's tensor-core MLP against a torch FP32 restatement of the same
+network (weights, inputs and hidden activations rounded to BF16 as the
+kernels do), finite differences on that restatement, online training.
+
+Tolerances: forward rtol 1e-2 / atol 2e-3 (BF16 operands, FP32 accumulation
+in a different order); gradients: cosine similarity > 0.995 and relative L2
+error < 5 % per tensor (the backward pass also rounds dZ to BF16).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def torch_model(p, x, round_acts=True):
+    import torch
+    from nuray_gb300.nrc import unpack
+    P = {k: torch.tensor(v) for k, v in unpack(p).items()}
+    bf = lambda a: a.to(torch.bfloat16).to(torch.float32)
+    h = bf(torch.tensor(x))
+    Ws = [bf(P[f"W{l}"]) for l in range(5)]
+    for l in range(4):
+        h = torch.relu(h @ Ws[l].T + P[f"b{l}"])
+        if round_acts:
+            h = bf(h)
+    return (h @ Ws[4].T + P["b4"])[:, :3]
+
+
+def rand_inputs(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, size=(n, 80)).astype(np.float32)
+    x[:, 72:80] = rng.uniform(0, 1, size=(n, 8))
+    return x
+
+
+def test_forward_matches_torch(gpu_lib):
+    from nuray_gb300.nrc import Cache
+    c = Cache("seed=3")
+    p = c.get_params()
+    x = rand_inputs(1000, 0)  # not a multiple of 16: ragged last tile
+    out = c.infer(x)
+    ref = torch_model(p, x).numpy()
+    np.testing.assert_allclose(out, ref, rtol=1e-2, atol=2e-3)
+    # random biases and output rows exercise every parameter
+    rng = np.random.default_rng(1)
+    p2 = p + rng.normal(scale=0.05, size=p.size).astype(np.float32)
+    from nuray_gb300.nrc import OFF
+    o, n = OFF["W4"]
+    p2[o + 3 * 64:o + n] = 0.0
+    o, n = OFF["b4"]
+    p2[o + 3:o + n] = 0.0
+    c.set_params(p2)
+    np.testing.assert_allclose(c.infer(x), torch_model(p2, x).numpy(), rtol=1e-2, atol=2e-3)
+    assert c.infer(x[:1]).shape == (1, 3)
+
+
+def test_gradient_matches_torch_and_finite_differences(gpu_lib):
+    import torch
+    from nuray_gb300.nrc import OFF, Cache, unpack
+    c = Cache("seed=5")
+    p = c.get_params()
+    rng = np.random.default_rng(2)
+    p = p + rng.normal(scale=0.02, size=p.size).astype(np.float32)
+    for k in ("W4", "b4"):
+        o, n = OFF[k]
+        rows = 64 if k == "W4" else 1
+        p[o + 3 * rows:o + n] = 0.0
+    c.set_params(p)
+    x = rand_inputs(777, 4)
+    y = rng.uniform(0, 2, size=(777, 3)).astype(np.float32)
+    g, loss = c.gradient(x, y)
+    # torch restatement of the loss; autograd through the FP32 model on BF16-rounded tensors
+    pt = torch.tensor(p, requires_grad=True)
+    from nuray_gb300.nrc import OFF as O
+
+    def loss_fn(pv):
+        parts = {k: pv[o:o + n] for k, (o, n) in O.items()}
+        bf = lambda a: a + (a.detach().to(torch.bfloat16).to(torch.float32) - a.detach())  # straight-through rounding
+        h = bf(torch.tensor(x))
+        for l in range(4):
+            W = parts[f"W{l}"].reshape(64, -1)
+            h = bf(torch.relu(h @ bf(W).T + parts[f"b{l}"]))
+        out = (h @ bf(parts["W4"].reshape(8, 64)).T + parts["b4"])[:, :3]
+        yt = torch.tensor(y)
+        return (((out - yt) ** 2) / (out.detach() ** 2 + 0.01)).mean()
+
+    L = loss_fn(pt)
+    L.backward()
+    gt = pt.grad.numpy()
+    assert abs(loss - L.item()) <= 2e-2 * abs(L.item())
+    for k, (o, n) in O.items():
+        a, b = g[o:o + n], gt[o:o + n]
+        if np.linalg.norm(b) < 1e-9:
+            assert np.linalg.norm(a) < 1e-6, k
+            continue
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
+        rel = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        assert cos > 0.995 and rel < 0.05, (k, cos, rel)
+    # central differences on the FP32 restatement confirm its gradient
+    with torch.no_grad():
+        for idx in [O["W0"][0] + 5, O["b1"][0] + 7, O["W3"][0] + 100, O["W4"][0] + 70, O["b4"][0] + 2]:
+            h = 1e-2
+            pp, pm = pt.detach().clone(), pt.detach().clone()
+            pp[idx] += h
+            pm[idx] -= h
+            fd = (loss_fn(pp) - loss_fn(pm)).item() / (2 * h)
+            assert abs(fd - gt[idx]) <= 0.05 * abs(gt[idx]) + 1e-4, (idx, fd, gt[idx])
+
+
+def test_training_reduces_loss(gpu_lib):
+    from nuray_gb300.nrc import Cache
+    c = Cache("seed=1 lr=3e-3")
+    rng = np.random.default_rng(7)
+    def target(x):
+        return np.stack([np.abs(np.sin(3 * x[:, 0])) + x[:, 76], 0.5 + 0.5 * np.cos(2 * x[:, 1] * x[:, 2]),
+                         x[:, 77] * x[:, 78]], 1).astype(np.float32)
+    xv = rand_inputs(4096, 99)
+    yv = target(xv)
+    first = c.gradient(xv, yv)[1]
+    for step in range(300):
+        x = rand_inputs(4096, step)
+        c.train_step(x, target(x))
+    last = c.gradient(xv, yv)[1]
+    assert last < 0.2 * first, (first, last)
+
+
+def cornell():
+    g = golden("cornell_scene.npz")
+    mats = [dict(type=int(i[0]), c0=f[0:3].tolist()) for i, f in zip(g["mat_i"], g["mat_f"])]
+    from nuray_gb300 import Scene
+    return Scene.from_arrays(g["pos"], g["mat"], mats, uv=g["uv"], nrm=g["nrm"])
+
+
+PARAMS = "renderer=ptnee imgw=64 imgh=48 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333 rrdepth=3 maxdepth=8"
+
+
+def test_train_only_mode_renders_plain_pt(gpu_lib):
+    from nuray_gb300.nrc import Cache
+    S = cornell()
+    plain = S.render(PARAMS)
+    c = Cache("seed=0")
+    c.attach(S)
+    p0 = c.get_params()
+    trained = S.render(PARAMS + " nrc=1 nrc_query=0 nrc_train=2048")
+    np.testing.assert_array_equal(plain, trained)  # paths unchanged, only recorded
+    assert not np.array_equal(p0, c.get_params())  # ... and the cache learned from them
+
+
+def test_nrc_render_close_to_reference(gpu_lib):
+    from nuray_gb300.nrc import Cache
+    S = cornell()
+    ref = S.render(PARAMS.replace("spp=16", "spp=2048") + " seed=7")
+    c = Cache("seed=0 lr=3e-3")
+    c.attach(S)
+    for k in range(30):  # warm up the cache on training paths
+        S.render(PARAMS + f" nrc=1 nrc_query=0 nrc_train=3072 sample0={16 * k}")
+    img = S.render(PARAMS + " nrc=1 nrc_train=3072 sample0=1000")
+    plain = S.render(PARAMS + " sample0=1000")
+    rel = lambda a: float(np.mean((a - ref) ** 2 / (ref ** 2 + 1e-2)))
+    print(f"relMSE at 16 spp: plain {rel(plain):.4f}, PT+NRC {rel(img):.4f}")
+    assert np.all(np.isfinite(img))
+    assert rel(img) < 0.1
+    assert abs(img.mean() / ref.mean() - 1) < 0.1
