@@ -27,6 +27,7 @@
  *   nr_material_probe                Material::bxdf/pdf/sampleBxdf (src/material/material.h:7-24)
  *   nr_nrc_*                         NNNodeMultiLayerPerceptron::eval / train (src/nn/nnnode.cpp:175-201)
  *   nr_scene_attach_nrc              RendererNRC's cache query (src/renderer/renderernrc.cpp:130-133)
+ *   nr_adjoint, nr_scene_set_materials  no reference counterpart (differentiation)
  *   nr_get_stats / nr_scene_stream   no reference counterpart (the reference reports only a
  *                                    wall-clock "secs used", src/renderer/rendererptls.cpp:232-233)
  */
@@ -250,6 +251,24 @@ int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, fl
  * prediction and trains the cache online on the suffix radiance of
  * nrc_train (default 16384) training paths per wavefront batch. NULL detaches. */
 int nr_scene_attach_nrc(nr_scene* scene, nr_nrc* nrc);
+
+/* ------------------------------------------------------------------------
+ * Differentiation (no counterpart in the reference).
+ * ------------------------------------------------------------------------ */
+
+/* Replaces the material parameters of a scene (same count, same types,
+ * emitters stay emitters) without rebuilding the BVH. */
+int nr_scene_set_materials(nr_scene* scene, int32_t n, const nr_material* mats);
+
+/* Path-replay adjoint of the ptnee estimator. Given dL_dimage = d loss /
+ * d image (W*H*3 floats, the image being the per-pixel mean of max(0, L)
+ * that nr_render returns for the same params), writes d loss / d params
+ * into dL_dparams: 7 floats per material (albedo r, g, b; roughness;
+ * emission r, g, b). Each path is re-traced from its Philox key instead of
+ * being stored. image (may be NULL) receives the primal image of the same
+ * samples. */
+int nr_adjoint(nr_scene* scene, const nr_camera* cam, const char* params, const float* dL_dimage, float* dL_dparams,
+               float* image);
 
 /* Material::bxdf, ::pdf and ::sampleBxdf of scene material `mat` evaluated
  * on the device for n queries: wo, nrm, wi, uv (3 floats each) and 4

@@ -79,6 +79,8 @@ SIGNATURES = {
     "nr_nrc_gradient": [_vp, _i32, _vp, _vp, _vp, _vp],
     "nr_nrc_train_step": [_vp, _i32, _vp, _vp, _vp],
     "nr_scene_attach_nrc": [_vp, _vp],
+    "nr_scene_set_materials": [_vp, _i32, _vp],
+    "nr_adjoint": [_vp, _vp, _cp, _vp, _vp, _vp],
 }
 
 _lib = None
@@ -231,6 +233,22 @@ class Scene:
         cam = ctypes.byref(camera) if camera is not None else None
         check(lib().nr_render_samples(self._h, cam, params.encode(), pix.shape[0], _ptr(pix), sample0, spp, _ptr(out)))
         return out
+
+    def set_materials(self, mats):
+        mt = (Material * len(mats))()
+        for i, m in enumerate(mats):
+            mt[i] = m if isinstance(m, Material) else make_material(**m)
+        check(lib().nr_scene_set_materials(self._h, len(mats), ctypes.addressof(mt)))
+
+    def adjoint(self, params, dl_dimage, camera=None, want_image=False):
+        """d loss / d (albedo rgb, roughness, emission rgb) per material, shape (num_mats, 7)."""
+        d = np.ascontiguousarray(dl_dimage, np.float32)
+        n = self.info()["mats"]
+        g = np.zeros((n, 7), np.float32)
+        img = np.zeros(d.shape, np.float32) if want_image else None
+        cam = ctypes.byref(camera) if camera is not None else None
+        check(lib().nr_adjoint(self._h, cam, params.encode(), _ptr(d), _ptr(g), _ptr(img)))
+        return (g, img) if want_image else g
 
     def stream(self):
         p = ctypes.c_void_p()

@@ -1,0 +1,261 @@
+// Path-replay adjoint of the ptnee estimator: d(loss)/d(per-material albedo,
+// roughness, emission) for a loss whose image gradient dL/dI the caller
+// provides. No per-vertex tape is kept: each path is traced twice from its
+// Philox key (pixel, sample). Pass 1 yields the path radiance L; pass 2
+// replays the same path and, at every factor that depends on a parameter,
+// adds delta . (d factor / d theta) . (radiance that factor multiplies), where
+// delta = dL/dI[pixel] / spp on the channels with L > 0 (the per-sample
+// max(0, .) of src/renderer/rendererptls.cpp:173) and the radiance after a
+// vertex is L minus what was accumulated before it (path replay
+// backpropagation, Vicini, Speierer and Jakob, SIGGRAPH 2021).
+//
+// Derivative terms (the estimator of RendererPTLS::trace, rendererptls.cpp:13-94):
+//  * albedo: f is affine in each channel of Kd (Lambert, GGXRefl F0, GGX F0,
+//    BlinnPhong Kd, glass F0), so d f_c / d Kd_c = f_c(Kd + 1) - f_c(Kd)
+//    exactly. Textured albedo has no gradient.
+//  * roughness: the sampled directions are held fixed (detached sampling:
+//    the 1/pdf of the sampling density is not differentiated, which keeps
+//    the estimator of d E[L] / d alpha unbiased); d f / d alpha and the
+//    derivative of the MIS weight through the BSDF pdf, including the
+//    (1 - mis) factor that weights the next emitter hit, use central
+//    differences of the device BSDF in alpha.
+//  * emission: linear; d/dKe of an emitter hit is T * fac, of an NEE term
+//    T * f * cos * mis / |lv|^2 * cos_l / p_light.
+#include "nr_material.cuh"
+#include "adjoint.h"
+
+namespace nr {
+
+namespace {
+
+struct GradAcc {
+    float* g;  // shared memory, num_mats * 7
+    __device__ void add(int m, int k, float v) {
+        if (v != 0.f) atomicAdd(&g[m * 7 + k], v);
+    }
+};
+
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// d f / d Kd per channel (f is affine in Kd).
+__device__ __forceinline__ f3 df_dkd(const MatView& M, f3 wo, f3 n, f3 wi, f3 f0) {
+    MatView P = M;
+    P.c0 = M.c0 + mk(1.f);
+    return mat_bxdf(P, wo, n, wi) - f0;
+}
+
+__device__ __forceinline__ bool has_alpha(const MatView& M) { return M.type == NR_MAT_GGXR || M.type == NR_MAT_GGX; }
+
+__device__ __forceinline__ float alpha_step(float a) { return fmaxf(1e-3f * a, 1e-5f); }
+
+__device__ __forceinline__ f3 df_dalpha(const MatView& M, f3 wo, f3 n, f3 wi) {
+    MatView P = M, Q = M;
+    float h = alpha_step(M.alpha);
+    P.alpha = M.alpha + h;
+    Q.alpha = M.alpha - h;
+    return (mat_bxdf(P, wo, n, wi) - mat_bxdf(Q, wo, n, wi)) / (2.f * h);
+}
+
+__device__ __forceinline__ float dpdf_dalpha(const MatView& M, f3 wo, f3 n, f3 wi) {
+    MatView P = M, Q = M;
+    float h = alpha_step(M.alpha);
+    P.alpha = M.alpha + h;
+    Q.alpha = M.alpha - h;
+    float a = mat_pdf(P, wo, n, wi), b = mat_pdf(Q, wo, n, wi);
+    if (a >= 1e17f || b >= 1e17f) return 0.f;  // the pdf's 1e18 sentinel branch
+    return (a - b) / (2.f * h);
+}
+
+// One path of the estimator. ADJ = false: returns its radiance. ADJ = true:
+// replays it and accumulates the parameter gradient into acc.
+template <bool ADJ>
+__device__ f3 replay(const AdjArgs& A, uint32_t key, uint32_t sample, int x, int y, f3 Ltot, f3 delta, GradAcc acc) {
+    const DeviceScene& S = A.S;
+    const Policy& pol = A.pol;
+    Stream rng;
+    rng.init(pol.seed_lo, pol.seed_hi, key, sample, 0);
+    float jx = rng.next();
+    float jy = rng.next();
+    f3 d = camera_ray(A.cam, A.film_h, (float)x + jx, (float)y + jy, (float)pol.imgw, (float)pol.imgh);
+    f3 o = mk(A.cam.pos[0], A.cam.pos[1], A.cam.pos[2]);
+    f3 T = mk(1.f), Lacc = mk(0.f);
+    float fac = 1.f, dfac_da = 0.f;
+    int prev_m = -1;
+    uint32_t dummy_err = 0;
+    for (int depth = 0;; ++depth) {
+        float t, b1, b2;
+        int tri = closest_hit(S, o, d, t, b1, b2, &dummy_err);
+        if (tri < 0) {
+            if (S.env_tex >= 0) Lacc = Lacc + T * env_lookup(S, d);
+            break;
+        }
+        float4 s0 = __ldg(&S.tri_shade[4 * tri]), s1 = __ldg(&S.tri_shade[4 * tri + 1]);
+        float4 s2 = __ldg(&S.tri_shade[4 * tri + 2]), s3 = __ldg(&S.tri_shade[4 * tri + 3]);
+        const int m = __float_as_int(s3.w);
+        float w0 = 1.0f - b1 - b2;
+        f3 normal = normalized(w0 * xyz(s0) + b1 * xyz(s1) + b2 * xyz(s2));
+        f3 wo = -d;
+        const int type = S.mats[m].type;
+        if (type == NR_MAT_LIGHT) {
+            const nr_material& E = S.mats[m];
+            f3 Ke = mk(E.c0[0], E.c0[1], E.c0[2]);
+            if (ADJ) {
+                f3 w = T * fac;
+                acc.add(m, 4, delta.x * w.x);
+                acc.add(m, 5, delta.y * w.y);
+                acc.add(m, 6, delta.z * w.z);
+                if (prev_m >= 0) acc.add(prev_m, 3, dot3(delta, T * Ke) * dfac_da);
+            }
+            Lacc = Lacc + T * Ke * fac;
+            break;
+        }
+        if (dot(normal, d) > 0.f && !mat_transmissive(type)) break;
+        f3 uv = mk(w0 * s0.w + b1 * s2.w + b2 * s3.y, w0 * s1.w + b1 * s3.x + b2 * s3.z, 0.f);
+        MatView M = load_mat(S, m, uv);
+        const bool textured = S.mats[m].tex0 >= 0;
+        f3 hit_pos = o + d * t;
+        fac = 1.f;
+        dfac_da = 0.f;
+        prev_m = m;
+        if (mat_nee(type) && S.num_lights > 0) {
+            float r = rng.next();
+            int lo = 0, hi = S.num_lights;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (__ldg(&S.light_cdf[mid]) < r) lo = mid + 1; else hi = mid;
+            }
+            int li = lo < S.num_lights ? lo : S.num_lights - 1;
+            const float4* L = S.lights + 6 * li;
+            float4 l0 = __ldg(&L[0]), l1 = __ldg(&L[1]), l2 = __ldg(&L[2]);
+            float4 n0 = __ldg(&L[3]), n1 = __ldg(&L[4]), n2 = __ldg(&L[5]);
+            float r1 = rng.next();
+            float r2 = rng.next();
+            if (r1 + r2 > 1.f) { r1 = 1.f - r1; r2 = 1.f - r2; }
+            float lw = 1.f - r1 - r2;
+            f3 light_pos = lw * xyz(l0) + r1 * xyz(l1) + r2 * xyz(l2);
+            f3 light_normal = normalized(lw * xyz(n0) + r1 * xyz(n1) + r2 * xyz(n2));
+            f3 light_vec = light_pos - hit_pos;
+            f3 wl = normalized(light_vec);
+            f3 Ke = mk(l0.w, l1.w, l2.w);
+            float light_pdf = S.light_p;
+            float cos_l = dot(light_normal, -wl);
+            float lop = light_pdf * dot(light_vec, light_vec) / smax(1e-6f, cos_l);
+            float bop = mat_pdf(M, wo, normal, wl);
+            float mis = lop / (lop + bop);
+            float dmis = 0.f;
+            if (ADJ && pol.mis && has_alpha(M)) dmis = -lop / ((lop + bop) * (lop + bop)) * dpdf_dalpha(M, wo, normal, wl);
+            if (!pol.mis) mis = 0.5f;
+            fac = 1.0f - mis;
+            dfac_da = -dmis;
+            f3 fl = mat_bxdf(M, wo, normal, wl);
+            float unit = 1.f / norm2(light_vec) * smax(0.f, cos_l) / light_pdf;
+            f3 Ll = Ke * unit;
+            float geo = smax(0.f, dot(normal, normalized(light_pos - hit_pos)));
+            f3 c = T * (Ll * fl * geo * mis);
+            // (pass 2 also needs visibility where c vanishes only through a zero albedo channel)
+            if (c.x != 0.f || c.y != 0.f || c.z != 0.f || (ADJ && unit * geo * mis > 0.f)) {
+                double lim = (double)norm(light_vec) - 2e-3;
+                float tmax = lim > 0.0 ? __double2float_rd(lim) : 0.0f;
+                bool visible = tmax <= 0.f || !any_hit(S, hit_pos + wl * 1e-3f, wl, tmax, &dummy_err);
+                if (visible) {
+                    if (ADJ) {
+                        if (!textured) {
+                            f3 dk = T * Ll * df_dkd(M, wo, normal, wl, fl) * (geo * mis);
+                            acc.add(m, 0, delta.x * dk.x);
+                            acc.add(m, 1, delta.y * dk.y);
+                            acc.add(m, 2, delta.z * dk.z);
+                        }
+                        if (has_alpha(M)) {
+                            f3 da = T * Ll * (df_dalpha(M, wo, normal, wl) * mis + fl * dmis) * geo;
+                            acc.add(m, 3, dot3(delta, da));
+                        }
+                        // the light's emission, material of the emitter triangle
+                        const int lm = __ldg(&S.light_mat[li]);
+                        f3 de = T * fl * (unit * geo * mis);
+                        acc.add(lm, 4, delta.x * de.x);
+                        acc.add(lm, 5, delta.y * de.y);
+                        acc.add(lm, 6, delta.z * de.z);
+                    }
+                    Lacc = Lacc + c;
+                }
+            }
+        }
+        if (pol.maxdepth > 0 && depth + 1 >= pol.maxdepth) break;
+        float prr = depth < pol.rrdepth ? 1.0f : pol.prr;
+        float u = rng.next();
+        if (depth >= pol.rrdepth && u > prr) break;
+        f3 wi = mat_sample(M, rng, wo, normal);
+        float pdf = mat_pdf(M, wo, normal, wi);
+        f3 f = mat_bxdf(M, wo, normal, wi);
+        if (ADJ) {
+            f3 after = Ltot - Lacc;  // radiance of the events this factor multiplies
+            if (!textured) {
+                f3 dk = df_dkd(M, wo, normal, wi, f);
+                if (f.x != 0.f) acc.add(m, 0, delta.x * after.x * dk.x / f.x);
+                if (f.y != 0.f) acc.add(m, 1, delta.y * after.y * dk.y / f.y);
+                if (f.z != 0.f) acc.add(m, 2, delta.z * after.z * dk.z / f.z);
+            }
+            if (has_alpha(M)) {
+                f3 da = df_dalpha(M, wo, normal, wi);
+                float g = 0.f;
+                if (f.x != 0.f) g += delta.x * after.x * da.x / f.x;
+                if (f.y != 0.f) g += delta.y * after.y * da.y / f.y;
+                if (f.z != 0.f) g += delta.z * after.z * da.z / f.z;
+                acc.add(m, 3, g);
+            }
+        }
+        T = T * fabsf(dot(wi, normal)) * f / pdf / prr;
+        o = hit_pos + wi * 1e-3f;
+        d = wi;
+    }
+    return Lacc;
+}
+
+}  // namespace
+
+// One thread per path: pass 1 for L, pass 2 for the gradient. Block-level
+// gradient histogram in shared memory, flushed with one atomic per entry.
+__global__ void __launch_bounds__(128) k_adjoint(AdjArgs A, const float* __restrict__ dldi, float* __restrict__ grad,
+                                                 float* __restrict__ image_sum) {
+    extern __shared__ float sg[];
+    const int NG = A.S.num_mats * 7;
+    for (int i = threadIdx.x; i < NG; i += blockDim.x) sg[i] = 0.f;
+    __syncthreads();
+    GradAcc acc{sg};
+    const uint64_t total = (uint64_t)A.npix * (uint64_t)A.spp;
+    const float inv_spp = 1.0f / (float)A.spp;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t pidx = (uint32_t)(g % (uint64_t)A.npix);
+        uint32_t srel = (uint32_t)(g / (uint64_t)A.npix);
+        int x = (int)(pidx % (uint32_t)A.pol.imgw), y = (int)(pidx / (uint32_t)A.pol.imgw);
+        uint32_t key = (uint32_t)y * (uint32_t)A.pol.imgw + (uint32_t)x;
+        uint32_t sample = A.sample0 + srel;
+        f3 L = replay<false>(A, key, sample, x, y, mk(0.f), mk(0.f), acc);
+        if (image_sum) {
+            atomicAdd(&image_sum[3 * pidx], smax(0.f, L.x));
+            atomicAdd(&image_sum[3 * pidx + 1], smax(0.f, L.y));
+            atomicAdd(&image_sum[3 * pidx + 2], smax(0.f, L.z));
+        }
+        f3 delta = mk(L.x > 0.f ? dldi[3 * pidx] * inv_spp : 0.f, L.y > 0.f ? dldi[3 * pidx + 1] * inv_spp : 0.f,
+                      L.z > 0.f ? dldi[3 * pidx + 2] * inv_spp : 0.f);
+        if (delta.x == 0.f && delta.y == 0.f && delta.z == 0.f) continue;
+        replay<true>(A, key, sample, x, y, L, delta, acc);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NG; i += blockDim.x)
+        if (sg[i] != 0.f) atomicAdd(&grad[i], sg[i]);
+}
+
+void adjoint_setup() { cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); }
+
+void launch_adjoint(const AdjArgs& A, const float* dldi, float* grad, float* image_sum, int num_sms, cudaStream_t st) {
+    const uint64_t total = (uint64_t)A.npix * (uint64_t)A.spp;
+    uint64_t blocks = (total + 127) / 128;
+    uint64_t cap = (uint64_t)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    size_t smem = (size_t)A.S.num_mats * 7 * sizeof(float);
+    k_adjoint<<<(unsigned)blocks, 128, smem, st>>>(A, dldi, grad, image_sum);
+}
+
+}  // namespace nr

@@ -17,6 +17,7 @@
 #include "host_scene.h"
 #include "integrator.h"
 #include "nrc.h"
+#include "adjoint.h"
 #include <random>
 
 namespace {
@@ -68,6 +69,10 @@ struct DevBuf {
         p = nullptr;
         bytes = 0;
     }
+    // keeps the current allocation when it is large enough
+    void ensure(size_t n) {
+        if (n > bytes) alloc(n);
+    }
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
@@ -109,7 +114,7 @@ struct nr_scene {
     nr::HostScene host;
     nr::Bvh bvh;
     nr::DeviceScene dev{};
-    DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf;
+    DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_mat;
     int num_gpu_nodes = 0;
     // wavefront state
     DevBuf path_mem, film, out_hdr, out_rgb8, pix_list, scratch;
@@ -128,8 +133,8 @@ struct nr_scene {
     ~nr_scene() {
         if (device >= 0) cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
-        for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &path_mem, &film,
-                        &out_hdr, &out_rgb8, &pix_list, &scratch, &nrc_mem})
+        for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_mat, &path_mem,
+                        &film, &out_hdr, &out_rgb8, &pix_list, &scratch, &nrc_mem})
             b->release();
         if (counters_host) cudaFreeHost(counters_host);
         for (auto& e : ev_pool) cudaEventDestroy(e);
@@ -204,6 +209,7 @@ void upload_scene(nr_scene* s) {
     // emitters in loader order, weight = Triangle::area (twice the area)
     std::vector<float4> lt;
     std::vector<float> pdf;
+    std::vector<int32_t> lmat;
     float sum = 0.0f;
     for (int i = 0; i < n; ++i) {
         const nr_material& M = H.mats[H.mat[i]];
@@ -215,6 +221,7 @@ void upload_scene(nr_scene* s) {
         float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
         float w = (float)std::sqrt((double)(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
         pdf.push_back(w);
+        lmat.push_back(H.mat[i]);
         sum += w;
         lt.push_back(make_float4(p[0], p[1], p[2], M.c0[0]));
         lt.push_back(make_float4(p[3], p[4], p[5], M.c0[1]));
@@ -250,6 +257,7 @@ void upload_scene(nr_scene* s) {
     upload(s->tex_info, tinfo, st);
     upload(s->lights, lt, st);
     upload(s->light_cdf, cdf, st);
+    upload(s->light_mat, lmat, st);
     NR_CUDA(cudaStreamSynchronize(st));
 
     nr::DeviceScene& D = s->dev;
@@ -261,6 +269,7 @@ void upload_scene(nr_scene* s) {
     D.tex_info = s->tex_info.as<int4>();
     D.lights = s->lights.as<float4>();
     D.light_cdf = s->light_cdf.as<float>();
+    D.light_mat = s->light_mat.as<int32_t>();
     D.num_lights = (int)pdf.size();
     D.light_p = (float)(1.0 / ((double)sum + 1e-8));
     D.num_tris = n;
@@ -381,6 +390,8 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgw = c.get_int("imgw", 1);
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
+    a.pol.trav = c.get_int("trav", 1);
+    if (a.pol.trav < 0 || a.pol.trav > 2) throw NrError(NR_ERR_INVALID, "trav must be 0, 1 or 2");
     a.wave = c.get_int("wave", 1 << 23);
     a.profile = c.get_int("profile", 0) != 0;
     a.count = c.get_int("count", 0) != 0;
@@ -651,6 +662,71 @@ int nr_scene_set_env(nr_scene* s, int32_t width, int32_t height, const float* rg
     });
 }
 
+int nr_scene_set_materials(nr_scene* s, int32_t n, const nr_material* mats) {
+    return guarded([&]() {
+        if (!s || !mats || n != (int32_t)s->host.mats.size()) throw NrError(NR_ERR_INVALID, "material count differs from the scene's");
+        for (int32_t m = 0; m < n; ++m) {
+            const nr_material& a = mats[m];
+            const nr_material& b = s->host.mats[m];
+            if (a.type != b.type) throw NrError(NR_ERR_INVALID, "material " + std::to_string(m) + ": type changed");
+            if ((a.type == NR_MAT_LIGHT) != (b.type == NR_MAT_LIGHT)) throw NrError(NR_ERR_INVALID, "emitters cannot change");
+            if (a.tex0 >= (int)s->host.tex_wh.size() / 2 || a.tex1 >= (int)s->host.tex_wh.size() / 2)
+                throw NrError(NR_ERR_INVALID, "material " + std::to_string(m) + ": texture index out of range");
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        s->host.mats.assign(mats, mats + n);
+        // emitter colours live in the emitter table as well: rebuild it with the materials
+        upload_scene(s);
+    });
+}
+
+int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const float* dldi, float* grad, float* image) {
+    return guarded([&]() {
+        if (!s || !dldi || !grad) throw NrError(NR_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        RenderArgs A = parse_args(cam, params);
+        const int npix = A.pol.imgw * A.pol.imgh;
+        const int nm = (int)s->host.mats.size();
+        if ((size_t)nm * 7 * 4 > 200 * 1024) throw NrError(NR_ERR_INVALID, "too many materials for the adjoint (limit 7314)");
+        cudaStream_t st = s->stream;
+        size_t b_img = (size_t)npix * 12, b_grad = (size_t)nm * 7 * 4;
+        s->scratch.ensure(2 * b_img + b_grad + 3 * 256);
+        char* p = s->scratch.as<char>();
+        auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
+        float* d_dldi = (float*)take(b_img);
+        float* d_img = (float*)take(b_img);
+        float* d_grad = (float*)take(b_grad);
+        NR_CUDA(cudaMemcpyAsync(d_dldi, dldi, b_img, cudaMemcpyHostToDevice, st));
+        NR_CUDA(cudaMemsetAsync(d_img, 0, b_img, st));
+        NR_CUDA(cudaMemsetAsync(d_grad, 0, b_grad, st));
+        nr::AdjArgs J;
+        J.S = s->dev;
+        J.pol = A.pol;
+        J.cam = A.cam;
+        J.film_h = nr::film_height(A.cam);
+        J.npix = npix;
+        J.sample0 = (uint32_t)A.sample0;
+        J.spp = A.spp;
+        static bool attr = false;
+        if (!attr) {
+            nr::adjoint_setup();
+            attr = true;
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        nr::launch_adjoint(J, d_dldi, d_grad, image ? d_img : nullptr, s->num_sms, st);
+        NR_CUDA(cudaGetLastError());
+        NR_CUDA(cudaMemcpyAsync(grad, d_grad, b_grad, cudaMemcpyDeviceToHost, st));
+        if (image) NR_CUDA(cudaMemcpyAsync(image, d_img, b_img, cudaMemcpyDeviceToHost, st));
+        NR_CUDA(cudaStreamSynchronize(st));
+        if (image) for (size_t i = 0; i < (size_t)npix * 3; ++i) image[i] /= (float)A.spp;
+        s->stats = nr_stats{};
+        s->stats.paths = (uint64_t)npix * A.spp;
+        s->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
 int nr_scene_info(const nr_scene* s, int64_t info[6]) {
     return guarded([&]() {
         if (!s || !info) throw NrError(NR_ERR_INVALID, "null argument");
@@ -707,7 +783,7 @@ int nr_intersect(nr_scene* s, int32_t n, const float* o, const float* d, int32_t
         float *dT = t, *dB1 = b1, *dB2 = b2;
         if (!(flags & NR_PTR_DEVICE)) {
             size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4;
-            s->scratch.alloc(2 * f3 + 4 * f1 + 6 * 256);  // six 256-byte aligned pieces
+            s->scratch.ensure(2 * f3 + 4 * f1 + 6 * 256);  // six 256-byte aligned pieces
             char* p = s->scratch.as<char>();
             auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
             float* xo = (float*)take(f3);
@@ -751,12 +827,12 @@ int nr_render(nr_scene* s, const nr_camera* cam, const char* params, float* hdr_
         RenderArgs A = parse_args(cam, params);
         const int npix = A.pol.imgw * A.pol.imgh;
         cudaStream_t st = s->stream;
-        s->film.alloc((size_t)npix * sizeof(float4));
+        s->film.ensure((size_t)npix * sizeof(float4));
         NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
         run_waves(s, A, npix, nullptr, A.sample0, s->film.as<float4>(), nullptr, cancel, progress, user);
         if (hdr_rgb || rgb8) {
-            if (hdr_rgb && s->out_hdr.bytes < (size_t)npix * 12) s->out_hdr.alloc((size_t)npix * 12);
-            if (rgb8 && s->out_rgb8.bytes < (size_t)npix * 3) s->out_rgb8.alloc((size_t)npix * 3);
+            if (hdr_rgb) s->out_hdr.ensure((size_t)npix * 12);
+            if (rgb8) s->out_rgb8.ensure((size_t)npix * 3);
             nr::launch_finish(s->film.as<float4>(), npix, 1.0f / (float)A.spp, hdr_rgb ? s->out_hdr.as<float>() : nullptr,
                               rgb8 ? s->out_rgb8.as<uint8_t>() : nullptr, st);
             if (hdr_rgb) NR_CUDA(cudaMemcpyAsync(hdr_rgb, s->out_hdr.p, (size_t)npix * 12, cudaMemcpyDeviceToHost, st));
@@ -780,8 +856,8 @@ int nr_render_samples(nr_scene* s, const nr_camera* cam, const char* params, int
                 throw NrError(NR_ERR_INVALID, "pixel outside the image");
         cudaStream_t st = s->stream;
         size_t nout = (size_t)npix * spp * 3;
-        s->pix_list.alloc((size_t)npix * 8);
-        s->out_hdr.alloc(nout * 4);
+        s->pix_list.ensure((size_t)npix * 8);
+        s->out_hdr.ensure(nout * 4);
         NR_CUDA(cudaMemcpyAsync(s->pix_list.p, pix_xy, (size_t)npix * 8, cudaMemcpyHostToDevice, st));
         run_waves(s, A, npix, s->pix_list.as<int32_t>(), sample0, nullptr, s->out_hdr.as<float>(), nullptr, nullptr, nullptr);
         NR_CUDA(cudaMemcpyAsync(out, s->out_hdr.p, nout * 4, cudaMemcpyDeviceToHost, st));
@@ -955,7 +1031,7 @@ int nr_material_probe(nr_scene* s, int32_t mat, int32_t n, const float* wo, cons
         NR_CUDA(cudaSetDevice(s->device));
         cudaStream_t st = s->stream;
         size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4, f4 = (size_t)n * 16;
-        s->scratch.alloc(4 * f3 + f4 + 2 * f3 + f1 + 8 * 256);  // eight 256-byte aligned pieces
+        s->scratch.ensure(4 * f3 + f4 + 2 * f3 + f1 + 8 * 256);  // eight 256-byte aligned pieces
         char* p = s->scratch.as<char>();
         auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
         float *dwo = (float*)take(f3), *dn = (float*)take(f3), *dwi = (float*)take(f3), *duv = (float*)take(f3);

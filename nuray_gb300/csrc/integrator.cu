@@ -81,6 +81,66 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
     if ((threadIdx.x & 31) == 0) atomicAdd(reinterpret_cast<unsigned long long*>(lohi), x);
 }
 
+// Closest hit, persistent: warps take 32 queue entries at a time from a
+// shared cursor, one ray per lane to completion (closest_hit). FAST selects
+// the tests with exact fallback; both give the same hits.
+template <bool COUNT, bool FAST>
+__global__ void __launch_bounds__(128) k_trace_batch(PathState P, DeviceScene S, int capacity) {
+    const uint32_t n = P.counters[CNT_IN];
+    const int lane = threadIdx.x & 31;
+    uint32_t nv = 0, nt = 0;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t idx = base + lane;
+        if (idx < n) {
+            int slot = P.queue_in[idx];
+            f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
+            float t, b1, b2;
+            int tri = closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                        COUNT ? &nt : nullptr);
+            P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
+            int cat = CAT_MISS;
+            if (tri >= 0) cat = S.mats[__float_as_int(__ldg(&S.tri_geo[3 * tri + 1]).w)].type;
+            int pos = warp_append_keyed(cat, &P.counters[CNT_CAT]);
+            P.sorted[(size_t)cat * capacity + pos] = slot;
+        }
+    }
+    if (COUNT) {
+        warp_count(nv, &P.counters[CNT_NODES]);
+        warp_count(nt, &P.counters[CNT_TRIS]);
+    }
+}
+
+template <bool COUNT, bool FAST>
+__global__ void __launch_bounds__(128) k_shadow_batch(PathState P, DeviceScene S) {
+    const uint32_t n = P.counters[CNT_SHADOW];
+    const int lane = threadIdx.x & 31;
+    uint32_t nv = 0, nt = 0;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK_SH], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        uint32_t idx = base + lane;
+        if (idx < n) {
+            float4 o = P.sh_o[idx], d = P.sh_d[idx];
+            if (!any_hit<FAST>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr, COUNT ? &nt : nullptr)) {
+                int slot = __float_as_int(d.w);
+                float4 c = P.sh_c[idx];
+                float4 r = P.rad[slot];
+                P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+            }
+        }
+    }
+    if (COUNT) {
+        warp_count(nv, &P.counters[CNT_SH_NODES]);
+        warp_count(nt, &P.counters[CNT_SH_TRIS]);
+    }
+}
+
 // Traversal state of one lane; the stack lives in local memory.
 struct Trav {
     int ref;       // next subtree, or NR_END
@@ -605,8 +665,8 @@ static int g_trace_blocks = 0, g_shadow_blocks = 0;
 
 void launch_setup(int num_sms) {
     int b1 = 0, b2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_trace<false>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_shadow<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_trace_batch<false, true>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_shadow_batch<false, true>, 128, 0);
     g_trace_blocks = num_sms * (b1 > 0 ? b1 : 1);
     g_shadow_blocks = num_sms * (b2 > 0 ? b2 : 1);
 }
@@ -619,16 +679,28 @@ void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, 
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc) {
     if (ev) cudaEventRecord(ev[0], st);
-    if (count) k_trace<true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
-    else k_trace<false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
+    switch ((count ? 4 : 0) + pol.trav) {
+        case 0: k_trace_batch<false, false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
+        case 1: k_trace_batch<false, true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
+        case 2: k_trace<false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
+        case 4: k_trace_batch<true, false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
+        case 5: k_trace_batch<true, true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
+        default: k_trace<true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
+    }
     if (ev) cudaEventRecord(ev[1], st);
     int shade_blocks = (max_count + 127) / 128;
     if (shade_blocks < 1) shade_blocks = 1;
     if (nrc) k_shade<true><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, *nrc);
     else k_shade<false><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, NrcCtx{});
     if (ev) cudaEventRecord(ev[2], st);
-    if (count) k_shadow<true><<<g_shadow_blocks, 128, 0, st>>>(P, S);
-    else k_shadow<false><<<g_shadow_blocks, 128, 0, st>>>(P, S);
+    switch ((count ? 4 : 0) + pol.trav) {
+        case 0: k_shadow_batch<false, false><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+        case 1: k_shadow_batch<false, true><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+        case 2: k_shadow<false><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+        case 4: k_shadow_batch<true, false><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+        case 5: k_shadow_batch<true, true><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+        default: k_shadow<true><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+    }
     if (ev) cudaEventRecord(ev[3], st);
     k_advance<<<1, 1, 0, st>>>(P.counters);
 }

@@ -229,6 +229,7 @@ __device__ __forceinline__ bool tri_test_fast(f3 o, f3 d, float4 g0, float4 g1, 
 // within a leaf, towards the earlier triangle. Visits children near-first
 // and prunes with the margin above. Returns the flattened triangle index or
 // -1; err is set on a stack overflow.
+template <bool FAST = true>
 __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, float& best_t, float& best_b1,
                                            float& best_b2, uint32_t* err, uint32_t* nodes_visited = nullptr,
                                            uint32_t* tris_tested = nullptr) {
@@ -254,8 +255,8 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
             int4 k = __ldg(&N.d);
             ++nv;
             float t0, t1;
-            bool h0 = box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
-            bool h1 = box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
+            bool h0 = FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
+            bool h1 = FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
             float lim = best_t * (1.0f + NR_PRUNE_MARGIN);
             h0 = h0 && t0 <= lim;
             h1 = h1 && t1 <= lim;
@@ -279,7 +280,9 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
                 float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
                 ++nt;
                 float t, u, v;
-                if (tri_test_fast(o, d, g0, g1, g2, lt, t, u, v)) { lt = t; lb1 = u; lb2 = v; li = ti; }
+                if (FAST ? tri_test_fast(o, d, g0, g1, g2, lt, t, u, v) : tri_test(o, d, g0, g1, g2, lt, t, u, v)) {
+                    lt = t; lb1 = u; lb2 = v; li = ti;
+                }
             }
             if (li >= 0 && (lt < best_t || (lt == best_t && first > best_leaf))) {
                 best_t = lt; best_b1 = lb1; best_b2 = lb2; best = li; best_leaf = first;
@@ -301,6 +304,7 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
 // Shadow query: true when some reachable triangle has a reference hit with
 // t <= tmax (the complement of `t + 2e-3 > |light_vec|` of
 // src/renderer/rendererptls.cpp:71 for the closest hit).
+template <bool FAST = true>
 __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float tmax, uint32_t* err,
                                         uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr) {
     if (S.root_ref == INT32_MIN) return false;
@@ -321,8 +325,8 @@ __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float 
             int4 k = __ldg(&N.d);
             if (nodes_visited) ++*nodes_visited;
             float t0, t1;
-            bool h0 = box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) && t0 <= lim;
-            bool h1 = box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) && t1 <= lim;
+            bool h0 = (FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0)) && t0 <= lim;
+            bool h1 = (FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1)) && t1 <= lim;
             if (h0 && h1) {
                 int nr = k.x, fr = k.y;
                 if (t1 < t0) { nr = k.y; fr = k.x; }
@@ -340,7 +344,7 @@ __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float 
                 float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
                 if (tris_tested) ++*tris_tested;
                 float t, u, v;
-                if (tri_test_fast(o, d, g0, g1, g2, limit, t, u, v)) return true;
+                if (FAST ? tri_test_fast(o, d, g0, g1, g2, limit, t, u, v) : tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
             }
         }
         if (sp == 0) break;

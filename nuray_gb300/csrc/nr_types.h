@@ -43,6 +43,7 @@ struct DeviceScene {
     const int4* tex_info;     // (w, h, texel offset, 0)
     const float4* lights;     // 6 per emitter: (p0, Ke.x) (p1, Ke.y) (p2, Ke.z) (n0,0) (n1,0) (n2,0)
     const float* light_cdf;
+    const int32_t* light_mat;  // material index of each emitter
     int32_t num_lights;
     float light_p;            // LightSampler::p()
     int32_t root_ref;         // root as a child reference; INT32_MIN for an empty scene
@@ -63,6 +64,7 @@ struct Policy {
     int32_t maxdepth; // 0 = unbounded (reference)
     uint32_t seed_lo, seed_hi;
     int32_t imgw, imgh;
+    int32_t trav;     // traversal kernel: 0 batch + exact tests, 1 batch + fast tests, 2 lane refill
 };
 
 // Wavefront path state, structure of arrays, one slot per in-flight path.
