@@ -6,8 +6,8 @@ One step renders one full frame of the workload: the seeded 1M-triangle
 terrain + spheres scene, 1920x1080, 64 samples per pixel, max depth 8,
 Russian roulette from depth 3, Philox seed 0 (132.7 M camera paths). The
 scene (BVH, triangles, materials) and the path state live in HBM; both are
-larger than the 129 MB L2 (about 150 MB of scene and 380 MB of path state
-per wavefront batch), so no L2 flush is inserted between steps.
+larger than the 129 MB L2 (about 150 MB of scene and 5.8 GB of path state
+per wavefront batch of 2^25 paths), so no L2 flush is inserted between steps.
 
 value: paths / s with the scene resident and the image left on the device
 (nr_render with no host output), timed with CUDA events on the library's
@@ -311,7 +311,7 @@ def main():
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded procedural scene; the reference publishes no benchmark scene)",
            "config": {"workload": desc, "triangles": int(sc["pos"].shape[0]), "paths_per_step": w * h * spp,
-                      "l2": "inputs larger than L2 (scene ~150 MB, path state ~380 MB per batch); no flush",
+                      "l2": "inputs larger than L2 (scene ~150 MB, path state ~5.8 GB per batch); no flush",
                       "parallelism": f"{world} rank(s), disjoint sample ranges, no collective on the data path",
                       "scene_build_s": round(build_s, 2)},
            "rays_per_s": round((rays + shadow_rays) / (ms / 1e3), 1), "extension_rays": rays,

@@ -193,7 +193,9 @@ int nr_camera_from_params(const char* params, nr_camera* cam);
  * imgw imgh spp prr mis (reference keys and defaults) plus seed (Philox seed,
  * default 0), rrdepth (first vertex where Russian roulette applies, default 0
  * as in the reference), maxdepth (0 = unbounded as in the reference),
- * wave (paths per wavefront batch, default 2^23), sample0 (index of the first
+ * wave (paths per wavefront batch, default 2^25), trav (0: traversal with
+ * the reference's exact arithmetic only, 1: fast tests with exact fallback,
+ * default; both return the same hits), sample0 (index of the first
  * sample, default 0: renders of disjoint sample ranges are independent and
  * their films sum), profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
  * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8

@@ -391,8 +391,8 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
     a.pol.trav = c.get_int("trav", 1);
-    if (a.pol.trav < 0 || a.pol.trav > 2) throw NrError(NR_ERR_INVALID, "trav must be 0, 1 or 2");
-    a.wave = c.get_int("wave", 1 << 23);
+    if (a.pol.trav < 0 || a.pol.trav > 1) throw NrError(NR_ERR_INVALID, "trav must be 0 or 1");
+    a.wave = c.get_int("wave", 1 << 25);
     a.profile = c.get_int("profile", 0) != 0;
     a.count = c.get_int("count", 0) != 0;
     a.sample0 = c.get_int("sample0", 0);

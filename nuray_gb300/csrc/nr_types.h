@@ -64,7 +64,7 @@ struct Policy {
     int32_t maxdepth; // 0 = unbounded (reference)
     uint32_t seed_lo, seed_hi;
     int32_t imgw, imgh;
-    int32_t trav;     // traversal kernel: 0 batch + exact tests, 1 batch + fast tests, 2 lane refill
+    int32_t trav;     // traversal tests: 0 exact arithmetic only, 1 fast path with exact fallback (same hits)
 };
 
 // Wavefront path state, structure of arrays, one slot per in-flight path.

@@ -176,6 +176,17 @@ def test_render_api_consistency(gpu_lib):
     np.testing.assert_array_equal(hdr, hdr2)
 
 
+def test_fast_traversal_tests_equal_exact_ones(gpu_lib):
+    """trav=1 (approximate tests with exact fallback) must return the hits of
+    trav=0 (the reference arithmetic throughout), so the images are identical."""
+    for sc, params in ((cornell_scene(), CORNELL.replace("imgw=320 imgh=240", "imgw=96 imgh=72")),
+                       (scenes.small_scene(3), scenes.small_scene(3)["params"])):
+        S = gpu_scene(sc)
+        a = S.render(params + " trav=0")
+        b = S.render(params + " trav=1")
+        np.testing.assert_array_equal(a, b)
+
+
 def test_errors_and_cancel(gpu_lib):
     import ctypes
     from nuray_gb300 import NuRayError
