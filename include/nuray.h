@@ -189,6 +189,24 @@ int nr_intersect(nr_scene* scene, int32_t n, const float* o, const float* d, int
  * (defaults 0,0,0 / 0,0,0 / 90 / 1). */
 int nr_camera_from_params(const char* params, nr_camera* cam);
 
+/* nr_intersect for host arrays without any device allocation by the library
+ * (no counterpart in the reference, which has no device memory at all).
+ * For callers that cannot let a library allocate device memory while they
+ * run: hosts that hand a plugin a fixed memory budget at start-up, or
+ * real-time loops that cannot take cudaMalloc's implicit device
+ * synchronisation mid-frame. Rays and results go through one static device
+ * array of NR_NOALLOC_MAX_RAYS (65,536) rays, 2.6 MB, reserved on every device
+ * that loads the library until the process exits; larger n is rejected with
+ * NR_ERR_INVALID (split the batch). The scene itself must already exist.
+ * The first call on a device looks up the array's device address (with that
+ * device current); make that first call before any stream capture. All calls
+ * share the array, which keeps the last call's contents; calls whose work
+ * overlapped on the GPU would race on it, so the library serialises them and
+ * returns only once the results are on the host. */
+#define NR_NOALLOC_MAX_RAYS 65536
+int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float* d, int32_t* tri, float* t, float* b1,
+                         float* b2);
+
 /* Renders the image. params uses the reference grammar ("key=value ..."):
  * imgw imgh spp prr mis (reference keys and defaults) plus seed (Philox seed,
  * default 0), rrdepth (first vertex where Russian roulette applies, default 0

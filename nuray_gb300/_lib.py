@@ -81,6 +81,7 @@ SIGNATURES = {
     "nr_scene_attach_nrc": [_vp, _vp],
     "nr_scene_set_materials": [_vp, _i32, _vp],
     "nr_adjoint": [_vp, _vp, _cp, _vp, _vp, _vp],
+    "nr_intersect_noalloc": [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
 }
 
 _lib = None

@@ -18,6 +18,7 @@
 #include "integrator.h"
 #include "nrc.h"
 #include "adjoint.h"
+#include "noalloc.h"
 #include <random>
 
 namespace {
@@ -808,6 +809,20 @@ int nr_intersect(nr_scene* s, int32_t n, const float* o, const float* d, int32_t
         NR_CUDA(cudaStreamSynchronize(st));
         err = s->counters_host[0];
         if (err) throw NrError(NR_ERR_DEVICE, "traversal error bits " + std::to_string(err) + " (1 stack overflow, 2 step cap)");
+    });
+}
+
+int nr_intersect_noalloc(nr_scene* s, int32_t n, const float* o, const float* d, int32_t* tri, float* t, float* b1,
+                         float* b2) {
+    return guarded([&]() {
+        if (!s || n < 0 || (n > 0 && (!o || !d || !tri || !t || !b1 || !b2))) throw NrError(NR_ERR_INVALID, "bad argument");
+        if (n > NR_NOALLOC_MAX_RAYS)
+            throw NrError(NR_ERR_INVALID, "nr_intersect_noalloc takes at most " + std::to_string(NR_NOALLOC_MAX_RAYS) +
+                                              " rays per call (got " + std::to_string(n) + "); split the batch");
+        std::lock_guard<std::mutex> lk(s->mu);
+        NR_CUDA(cudaSetDevice(s->device));
+        std::string err = nr::noalloc_intersect(s->dev, s->device, s->stream, n, o, d, tri, t, b1, b2);
+        if (!err.empty()) throw NrError(err.rfind("traversal", 0) == 0 ? NR_ERR_DEVICE : NR_ERR_CUDA, err);
     });
 }
 
