@@ -213,7 +213,9 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * as in the reference), maxdepth (0 = unbounded as in the reference),
  * wave (paths per wavefront batch, default 2^25), trav (0: traversal with
  * the reference's exact arithmetic only, 1: fast tests with exact fallback,
- * default; both return the same hits), sample0 (index of the first
+ * default; both return the same hits), accumulate=1 (add to the film of
+ * the previous call of the same size instead of clearing it; the outputs are
+ * the mean over all samples added so far), sample0 (index of the first
  * sample, default 0: renders of disjoint sample ranges are independent and
  * their films sum), profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
  * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
@@ -267,9 +269,13 @@ int nr_nrc_gradient(nr_nrc* nrc, int32_t n, const float* x, const float* y, floa
  * mean loss before the step. */
 int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, float* loss);
 /* Attaches a cache to a scene: nr_render with nrc=1 then ends non-training
- * paths at the vertex after their first diffuse bounce with the cache's
- * prediction and trains the cache online on the suffix radiance of
- * nrc_train (default 16384) training paths per wavefront batch. NULL detaches. */
+ * paths at the vertex after their first diffuse bounce (a Lambert or
+ * BlinnPhong vertex, or GGX with roughness >= nrc_rough, default 0.2), at
+ * vertex depth >= nrc_mindepth (default 1), with the cache's prediction, and
+ * trains the cache online on the suffix radiance of nrc_train (default
+ * 16384) training paths per wavefront batch in nrc_steps (default 4) Adam
+ * steps; nrc_query=0 only trains. NULL detaches. The cache must not be used
+ * through nr_nrc_* while a render of the scene runs. */
 int nr_scene_attach_nrc(nr_scene* scene, nr_nrc* nrc);
 
 /* ------------------------------------------------------------------------

@@ -19,55 +19,66 @@ def relmse(img, ref):
     return float(np.mean((a - r) ** 2 / (r ** 2 + 1e-2)))
 
 
-def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", time_limit_s=60.0):
-    """Renders up to `frames` 1-spp frames; returns the relMSE curve as
-    (elapsed_ms, spp, relmse) rows and the time at which `target` is met."""
+def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", time_limit_s=60.0, growth=1.03):
+    """Renders up to `frames` 1-spp frames, accumulated on the device; the
+    image is read back and compared at checkpoints spaced by `growth` in
+    sample count. Returns (elapsed_ms, spp, relmse) rows and the elapsed GPU
+    time at the first checkpoint that meets `target`."""
     import torch
     stream = torch.cuda.ExternalStream(scene.stream())
-    acc = None
     curve = []
     hit = None
     elapsed = 0.0
+    next_check = 1.0
     t_wall = time.perf_counter()
     for k in range(frames):
-        p = params.replace("spp=", "spp_unused=") + f" spp=1 sample0={k}"
+        p = params.replace("spp=", "spp_unused=") + f" spp=1 sample0={k}" + (" accumulate=1" if k else "")
         if nrc is not None:
             p += " nrc=1 " + nrc_params
+        check = k + 1 >= next_check or k == frames - 1
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        img = scene.render(p)
+        img = scene.render(p) if check else scene.render_device(p)
         e1.record(stream)
         e1.synchronize()
         elapsed += e0.elapsed_time(e1)
-        acc = img.astype(np.float64) if acc is None else acc + img
-        err = relmse(acc / (k + 1), ref)
-        curve.append((round(elapsed, 2), k + 1, err))
-        if hit is None and err <= target:
-            hit = elapsed
-            break
+        if check:
+            next_check = max(next_check * growth, k + 2)
+            err = relmse(img, ref)
+            curve.append((round(elapsed, 2), k + 1, err))
+            if err <= target:
+                hit = elapsed
+                break
         if time.perf_counter() - t_wall > time_limit_s:
             break
     return curve, hit
 
 
-def compare(scene, params, target=1e-3, ref_spp=4096, frames=4096, nrc_params="nrc_train=16384", seed_ref=12345,
-            time_limit_s=60.0):
-    """Returns a dict with the reference, the plain curve and the NRC curve."""
+def reference(scene, params, ref_spp=8192, seed_ref=12345):
+    return scene.render(params.replace("spp=", "spp_unused=") + f" spp={ref_spp} seed={seed_ref}")
+
+
+def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s):
+    from ._lib import check, lib
     from .nrc import Cache
-    ref = scene.render(params.replace("spp=", "spp_unused=") + f" spp={ref_spp} seed={seed_ref}")
-    pt_curve, pt_t = progressive(scene, params, frames, ref, target, time_limit_s=time_limit_s)
     cache = Cache("lr=1e-3 beta1=0.9 beta2=0.99")
     cache.attach(scene)
     try:
-        nrc_curve, nrc_t = progressive(scene, params, frames, ref, target, nrc=cache, nrc_params=nrc_params,
-                                       time_limit_s=time_limit_s)
+        return progressive(scene, params, frames, ref, target, nrc=cache, nrc_params=nrc_params,
+                           time_limit_s=time_limit_s)
     finally:
-        from ._lib import check, lib
         check(lib().nr_scene_attach_nrc(scene._h, None))
         cache.close()
-    return {"target": target, "ref_spp": ref_spp,
-            "pt": {"ms_to_target": None if pt_t is None else round(pt_t, 1), "frames": pt_curve[-1][1],
-                   "final_relmse": pt_curve[-1][2]},
-            "pt_nrc": {"ms_to_target": None if nrc_t is None else round(nrc_t, 1), "frames": nrc_curve[-1][1],
-                       "final_relmse": nrc_curve[-1][2]},
+
+
+def summary(curve, t):
+    return {"ms_to_target": None if t is None else round(t, 1), "frames": curve[-1][1], "final_relmse": curve[-1][2]}
+
+
+def compare(scene, params, target=1e-3, ref_spp=8192, frames=50000, nrc_params="nrc_train=16384", time_limit_s=60.0):
+    """Plain PT and PT + NRC against the same reference; returns both summaries and curves."""
+    ref = reference(scene, params, ref_spp)
+    pt_curve, pt_t = progressive(scene, params, frames, ref, target, time_limit_s=time_limit_s)
+    nrc_curve, nrc_t = run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s)
+    return {"target": target, "ref_spp": ref_spp, "pt": summary(pt_curve, pt_t), "pt_nrc": summary(nrc_curve, nrc_t),
             "pt_curve": pt_curve[:: max(1, len(pt_curve) // 32)], "nrc_curve": nrc_curve[:: max(1, len(nrc_curve) // 32)]}

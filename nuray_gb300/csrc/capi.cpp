@@ -119,6 +119,8 @@ struct nr_scene {
     int num_gpu_nodes = 0;
     // wavefront state
     DevBuf path_mem, film, out_hdr, out_rgb8, pix_list, scratch;
+    int film_pixels = 0;
+    uint64_t film_samples = 0;  // samples summed in film (accumulate=1 keeps adding)
     nr::PathState ps{};
     int capacity = 0;
     uint32_t* counters_host = nullptr;  // pinned
@@ -147,7 +149,8 @@ namespace {
 
 uint64_t device_bytes(const nr_scene* s) {
     uint64_t b = 0;
-    for (auto* x : {&s->nodes, &s->tri_geo, &s->tri_shade, &s->mats, &s->texels, &s->tex_info, &s->lights, &s->light_cdf})
+    for (auto* x : {&s->nodes, &s->tri_geo, &s->tri_shade, &s->mats, &s->texels, &s->tex_info, &s->lights, &s->light_cdf,
+                    &s->light_mat})
         b += x->bytes;
     return b;
 }
@@ -369,10 +372,12 @@ struct RenderArgs {
     bool profile;
     bool count;
     int sample0;
+    bool accumulate;
     bool nrc;
     int nrc_train;    // training paths per wavefront batch
     int nrc_steps;    // Adam steps per batch
     int nrc_query;    // 0: train only
+    int nrc_mindepth; // first vertex at which a path may end in the cache
     float nrc_rough;  // roughness from which a GGX vertex is diffuse
 };
 
@@ -397,10 +402,12 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.profile = c.get_int("profile", 0) != 0;
     a.count = c.get_int("count", 0) != 0;
     a.sample0 = c.get_int("sample0", 0);
+    a.accumulate = c.get_int("accumulate", 0) != 0;
     a.nrc = c.get_int("nrc", 0) != 0;
     a.nrc_train = c.get_int("nrc_train", 16384);
     a.nrc_steps = c.get_int("nrc_steps", 4);
     a.nrc_query = c.get_int("nrc_query", 1);
+    a.nrc_mindepth = c.get_int("nrc_mindepth", 1);
     a.nrc_rough = c.get_float("nrc_rough", 0.2f);
     if (a.nrc && (a.nrc_train <= 0 || a.nrc_steps <= 0)) throw NrError(NR_ERR_INVALID, "nrc_train and nrc_steps must be positive");
     if (a.sample0 < 0) throw NrError(NR_ERR_INVALID, "sample0 must be >= 0");
@@ -451,6 +458,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         X.tcap = s->nrc_tcap;
         X.train_stride = (uint32_t)std::max<int64_t>(1, (int64_t)cap / A.nrc_train);
         X.query = A.nrc_query;
+        X.min_depth = A.nrc_mindepth;
         X.rough = A.nrc_rough;
         for (int k = 0; k < 3; ++k) {
             float ext = s->dev.root_hi[k] - s->dev.root_lo[k];
@@ -843,12 +851,17 @@ int nr_render(nr_scene* s, const nr_camera* cam, const char* params, float* hdr_
         const int npix = A.pol.imgw * A.pol.imgh;
         cudaStream_t st = s->stream;
         s->film.ensure((size_t)npix * sizeof(float4));
-        NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
+        if (!A.accumulate || s->film_pixels != npix) {
+            NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
+            s->film_samples = 0;
+            s->film_pixels = npix;
+        }
         run_waves(s, A, npix, nullptr, A.sample0, s->film.as<float4>(), nullptr, cancel, progress, user);
+        s->film_samples += (uint64_t)A.spp;
         if (hdr_rgb || rgb8) {
             if (hdr_rgb) s->out_hdr.ensure((size_t)npix * 12);
             if (rgb8) s->out_rgb8.ensure((size_t)npix * 3);
-            nr::launch_finish(s->film.as<float4>(), npix, 1.0f / (float)A.spp, hdr_rgb ? s->out_hdr.as<float>() : nullptr,
+            nr::launch_finish(s->film.as<float4>(), npix, 1.0f / (float)s->film_samples, hdr_rgb ? s->out_hdr.as<float>() : nullptr,
                               rgb8 ? s->out_rgb8.as<uint8_t>() : nullptr, st);
             if (hdr_rgb) NR_CUDA(cudaMemcpyAsync(hdr_rgb, s->out_hdr.p, (size_t)npix * 12, cudaMemcpyDeviceToHost, st));
             if (rgb8) NR_CUDA(cudaMemcpyAsync(rgb8, s->out_rgb8.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, st));

@@ -85,8 +85,9 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // shared cursor, one ray per lane to completion (closest_hit), then the slot
 // is bucketed by shading category (material type of the hit, or CAT_MISS).
 // FAST selects the box / triangle tests with exact fallback; both variants
-// return the same hits bit for bit. (A variant that refilled idle lanes
-// from the queue and separated node and leaf phases measured 28 % slower.)
+// return the same hits bit for bit. (Measured and dropped: a variant that
+// refilled idle lanes from the queue with separate node and leaf phases,
+// 28 % slower; a four-wide tree collapsed from this one, no faster.)
 template <bool COUNT, bool FAST>
 __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int capacity) {
     const uint32_t n = P.counters[CNT_IN];
@@ -203,7 +204,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     uint32_t flags = meta.w & NR_META_SEEN_DIFFUSE;
     if (NRC) {
         const bool train = nrc_is_training(meta.x, meta.y, C.train_stride);
-        if (!train && flags && C.query) {
+        if (!train && flags && C.query && depth >= C.min_depth) {
             // past the first diffuse bounce: the cache stands in for the rest of the path
             int q = warp_append(true, &C.counters[0]);
             C.q_slot[q] = slot;

@@ -101,6 +101,7 @@ struct NrcCtx {
     int32_t tcap;
     uint32_t train_stride;  // one path in train_stride is a training path
     int32_t query;          // 0: train only (every path runs to the end)
+    int32_t min_depth;      // first vertex depth at which the cache may end a path
     float rough;            // GGX roughness from which a vertex counts as diffuse
     float lo[3], inv_ext[3];  // scene box for the position encoding
 };

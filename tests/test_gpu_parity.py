@@ -187,6 +187,15 @@ def test_fast_traversal_tests_equal_exact_ones(gpu_lib):
         np.testing.assert_array_equal(a, b)
 
 
+def test_accumulate_across_calls_equals_one_call(gpu_lib):
+    S = gpu_scene(cornell_scene())
+    params = "renderer=ptnee imgw=48 imgh=36 spp=4 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
+    once = S.render(params)
+    for k in range(4):
+        img = S.render(params.replace("spp=4", "spp=1") + f" sample0={k}" + (" accumulate=1" if k else ""))
+    np.testing.assert_allclose(img, once, rtol=1e-6, atol=1e-7)
+
+
 def test_errors_and_cancel(gpu_lib):
     import ctypes
     from nuray_gb300 import NuRayError
