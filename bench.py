@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-tile-stride", type=int, default=32, help="CPU sample: every k-th 4x4 tile")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+                    help="c2: the 1M-triangle scene (default); c3: the same with an HDR sky, value-noise "
+                         "textures on half the materials and 10%% GGX dielectrics, spp 256")
     return ap.parse_args()
 
 
@@ -73,13 +76,19 @@ def dist_env():
 def workload(args):
     from nuray_gb300 import scenes
     sc = scenes.terrain_spheres(0)
+    if args.workload == "c3":
+        sc = scenes.with_env_textures(sc, 0)
+        if args.spp == 64:
+            args.spp = 256
     w, h = (int(x) for x in args.res.split("x"))
     params = sc["params"].replace("imgw=1920", f"imgw={w}").replace("imgh=1080", f"imgh={h}")
-    params = params.replace("spp=64", f"spp={args.spp}")
+    params = params.replace("spp=64", f"spp={args.spp}").replace("spp=256", f"spp={args.spp}")
     if args.wave:
         params += f" wave={args.wave}"
     desc = (f"procedural terrain+spheres, {sc['pos'].shape[0]} triangles, {w}x{h}, spp={args.spp}, "
             "maxdepth 8, RR from depth 3, GGX-reflect materials, 32 quad lights, Philox seed 0")
+    if args.workload == "c3":
+        desc += ", 2048x1024 HDR sky (peak 5e3), 512x512 value-noise textures on half the materials, 10% GGX dielectrics"
     return sc, params, desc, w, h
 
 
@@ -211,7 +220,8 @@ def main():
     build.build()
     sc, params, desc, w, h = workload(args)
     t0 = time.perf_counter()
-    S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"])
+    S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"], textures=sc["textures"],
+                          env_tex=sc["env_tex"], env_gain=sc["env_gain"])
     build_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(S.stream())
     spp = args.spp

@@ -253,7 +253,10 @@ int nr_scene_stream(const nr_scene* scene, void** stream);
 typedef struct nr_nrc nr_nrc;
 
 /* params: lr (1e-3), beta1 (0.9), beta2 (0.99), eps (1e-8), seed (0, for the
- * Glorot-uniform initialisation). Allocates on the current device. */
+ * Glorot-uniform initialisation), ema (0.99: renders query an exponential
+ * moving average of the weights over Adam steps, 0 queries the current
+ * weights). Allocates on the current device. nr_nrc_infer and the
+ * gradient calls use the current weights. */
 int nr_nrc_create(const char* params, nr_nrc** out);
 int nr_nrc_destroy(nr_nrc* nrc);
 /* Number of FP32 parameters (weights and biases, layout in nrc.h). */

@@ -87,7 +87,7 @@ struct nr_nrc {
     cudaStream_t stream = nullptr;
     DevBuf pbuf;  // params | grad | m | v (FP32) then the BF16 copy
     nr::NrcDev dev{};
-    float lr = 1e-3f, b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+    float lr = 1e-3f, b1 = 0.9f, b2 = 0.99f, eps = 1e-8f, ema = 0.0f;
     int step = 0;
     // scratch for batches: x (BF16), y, out, acts, dz, loss
     DevBuf batch;
@@ -360,7 +360,7 @@ void nrc_train_device(nr_nrc* c, const __nv_bfloat16* x, const float* y, int m, 
     nr::nrc_launch_backward(c->dev, x, c->out, y, c->acts, c->dz, m, c->loss, c->num_sms, st);
     if (update) {
         c->step++;
-        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, st);
+        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, st);
     }
 }
 
@@ -373,6 +373,7 @@ struct RenderArgs {
     bool count;
     int sample0;
     bool accumulate;
+    bool tile;
     bool nrc;
     int nrc_train;    // training paths per wavefront batch
     int nrc_steps;    // Adam steps per batch
@@ -403,6 +404,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.count = c.get_int("count", 0) != 0;
     a.sample0 = c.get_int("sample0", 0);
     a.accumulate = c.get_int("accumulate", 0) != 0;
+    a.tile = c.get_int("tile", 1) != 0;
     a.nrc = c.get_int("nrc", 0) != 0;
     a.nrc_train = c.get_int("nrc_train", 16384);
     a.nrc_steps = c.get_int("nrc_steps", 4);
@@ -495,6 +497,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         W.npix = npix;
         W.sample0 = (uint32_t)sample0;
         W.pix_xy = dev_pix;
+        W.tiled = (!dev_pix && A.tile && A.pol.imgw % 8 == 0 && A.pol.imgh % 4 == 0) ? 1 : 0;
         mark(-1);
         // queue_in / queue_out swap roles every bounce
         nr::PathState P = s->ps;
@@ -541,8 +544,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             qt[1] = std::min<uint32_t>(s->counters_host[1], (uint32_t)s->nrc_tcap);
             nr_nrc* c = s->nrc;
             if (qt[0] > 0) {
-                nr::nrc_launch_forward(c->dev, (const __nv_bfloat16*)s->nrc_ctx.q_x, (int)qt[0], s->nrc_pred, nullptr,
-                                       c->num_sms, st);
+                nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)s->nrc_ctx.q_x, (int)qt[0], s->nrc_pred,
+                                           c->num_sms, st);
                 nr::launch_nrc_apply(s->ps, s->nrc_ctx, s->nrc_pred, (int)qt[0], st);
                 S.kernel_launches += 2;
             }
@@ -560,7 +563,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                     nr::nrc_launch_backward(c->dev, x, c->out, c->y + 3 * (size_t)m0, c->acts, c->dz, m, c->loss,
                                             c->num_sms, st);
                     c->step++;
-                    nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, st);
+                    nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, st);
                     S.kernel_launches += 9;
                 }
                 NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, st));
@@ -570,7 +573,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             }
         }
         mark(-1);
-        if (film) nr::launch_film(s->ps, W, film, st);
+        if (film) nr::launch_film(s->ps, W, film, A.pol.imgw, st);
         if (dev_out) nr::launch_collect(s->ps, W, dev_out, A.spp, st);
         S.kernel_launches += 1;
         mark(3);
@@ -922,15 +925,20 @@ int nr_nrc_create(const char* params, nr_nrc** out) {
         n->b1 = c.get_float("beta1", 0.9f);
         n->b2 = c.get_float("beta2", 0.99f);
         n->eps = c.get_float("eps", 1e-8f);
+        n->ema = c.get_float("ema", 0.99f);
+        if (n->ema < 0.f || n->ema >= 1.f) throw NrError(NR_ERR_INVALID, "ema must be in [0, 1)");
         nr::nrc_setup();
         const size_t P = NRC_NUM_PARAMS;
-        n->pbuf.alloc(4 * P * 4 + P * 2 + 256);
+        n->pbuf.alloc(6 * P * 4 + 2 * P * 2 + 512);
         float* f = n->pbuf.as<float>();
         n->dev.params = f;
         n->dev.grad = f + P;
         n->dev.m = f + 2 * P;
         n->dev.v = f + 3 * P;
-        n->dev.wb = reinterpret_cast<__nv_bfloat16*>(f + 4 * P);
+        n->dev.ema = f + 4 * P;
+        n->dev.pinf = f + 5 * P;
+        n->dev.wb = reinterpret_cast<__nv_bfloat16*>(f + 6 * P);
+        n->dev.wb_inf = n->dev.wb + P + 64;
         // Glorot-uniform weights, zero biases; output rows 3..7 stay zero
         std::vector<float> init(P, 0.0f);
         std::mt19937_64 rng((uint64_t)c.get_int("seed", 0));
@@ -947,8 +955,10 @@ int nr_nrc_create(const char* params, nr_nrc** out) {
         fill(NRC_OFF_W3, NRC_H, NRC_H, NRC_H);
         fill(NRC_OFF_W4, NRC_OUT_PAD, NRC_H, NRC_OUT);
         NR_CUDA(cudaMemcpyAsync(n->dev.params, init.data(), P * 4, cudaMemcpyHostToDevice, n->stream));
-        NR_CUDA(cudaMemsetAsync(n->dev.grad, 0, 3 * P * 4, n->stream));
+        NR_CUDA(cudaMemcpyAsync(n->dev.pinf, init.data(), P * 4, cudaMemcpyHostToDevice, n->stream));
+        NR_CUDA(cudaMemsetAsync(n->dev.grad, 0, 4 * P * 4, n->stream));  // grad, m, v, ema
         nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb, P, n->stream);
+        nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb_inf, P, n->stream);
         NR_CUDA(cudaStreamSynchronize(n->stream));
         *out = n.release();
     });
@@ -974,8 +984,10 @@ int nr_nrc_set_params(nr_nrc* n, const float* in) {
         std::lock_guard<std::mutex> lk(n->mu);
         NR_CUDA(cudaSetDevice(n->device));
         NR_CUDA(cudaMemcpyAsync(n->dev.params, in, NRC_NUM_PARAMS * 4, cudaMemcpyHostToDevice, n->stream));
-        NR_CUDA(cudaMemsetAsync(n->dev.grad, 0, 3 * (size_t)NRC_NUM_PARAMS * 4, n->stream));
+        NR_CUDA(cudaMemcpyAsync(n->dev.pinf, in, NRC_NUM_PARAMS * 4, cudaMemcpyHostToDevice, n->stream));
+        NR_CUDA(cudaMemsetAsync(n->dev.grad, 0, 4 * (size_t)NRC_NUM_PARAMS * 4, n->stream));
         nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb, NRC_NUM_PARAMS, n->stream);
+        nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb_inf, NRC_NUM_PARAMS, n->stream);
         n->step = 0;
         NR_CUDA(cudaStreamSynchronize(n->stream));
     });
@@ -1015,7 +1027,7 @@ static int nrc_grad_impl(nr_nrc* c, int32_t n, const float* x, const float* y, f
         if (grad) NR_CUDA(cudaMemcpyAsync(grad, c->dev.grad, NRC_NUM_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream));
         if (update) {
             c->step++;
-            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->stream);
+            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, c->stream);
         } else {
             NR_CUDA(cudaMemsetAsync(c->dev.grad, 0, NRC_NUM_PARAMS * 4, c->stream));
         }

@@ -41,6 +41,19 @@ __device__ __forceinline__ int warp_append_keyed(int key, uint32_t* counters) {
     return (int)(base + rank);
 }
 
+// Full-frame pixel of path index p: row-major, or in 8x4 tiles (one warp of
+// consecutive paths covers a compact patch) when the frame divides into them.
+__device__ __forceinline__ void frame_pixel(uint32_t p, int w, int tiled, int& x, int& y) {
+    if (tiled) {
+        uint32_t tile = p >> 5, j = p & 31u, tiles_x = (uint32_t)w >> 3;
+        x = (int)((tile % tiles_x) * 8u + (j & 7u));
+        y = (int)((tile / tiles_x) * 4u + (j >> 3));
+    } else {
+        x = (int)(p % (uint32_t)w);
+        y = (int)(p / (uint32_t)w);
+    }
+}
+
 // ---------------------------------------------------------------- ray generation
 // RendererPTLS::render per-sample body (src/renderer/rendererptls.cpp:170-173):
 // jitter x, jitter y, Camera::generateRay.
@@ -52,7 +65,7 @@ __global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, P
     uint32_t pidx = (uint32_t)(g % (uint64_t)W.npix);
     int x, y;
     if (W.pix_xy) { x = W.pix_xy[2 * pidx]; y = W.pix_xy[2 * pidx + 1]; }
-    else { x = (int)(pidx % (uint32_t)pol.imgw); y = (int)(pidx / (uint32_t)pol.imgw); }
+    else frame_pixel(pidx, pol.imgw, W.tiled, x, y);
     uint32_t key = (uint32_t)y * (uint32_t)pol.imgw + (uint32_t)x;
     uint32_t sample = W.sample0 + srel;
     Stream s;
@@ -340,22 +353,25 @@ __global__ void k_reset_counters(uint32_t* counters) {
 // ---------------------------------------------------------------- film
 // For every pixel of the wave, adds max(0, L) of its samples in sample order
 // (rendererptls.cpp:173). film holds npix float4 sums.
-__global__ void k_film(PathState P, WaveDesc W, float4* film) {
+__global__ void k_film(PathState P, WaveDesc W, float4* film, int imgw) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (uint32_t)W.npix) return;
+    int x, y;
+    frame_pixel(p, imgw, W.tiled, x, y);
+    const uint32_t pix = (uint32_t)y * (uint32_t)imgw + (uint32_t)x;
     uint64_t end = W.base + (uint64_t)W.count;
     uint64_t s_first = W.base / (uint64_t)W.npix;
     uint64_t g = s_first * (uint64_t)W.npix + p;
     if (g < W.base) g += (uint64_t)W.npix;
     if (g >= end) return;
-    float4 acc = film[p];
+    float4 acc = film[pix];
     for (; g < end; g += (uint64_t)W.npix) {
         float4 r = P.rad[g - W.base];
         acc.x += smax(0.f, r.x);
         acc.y += smax(0.f, r.y);
         acc.z += smax(0.f, r.z);
     }
-    film[p] = acc;
+    film[pix] = acc;
 }
 
 // Copies per-sample max(0, L) to out[(pixel * spp + sample) * 3].
@@ -495,8 +511,8 @@ void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, int n, fl
     if (n > 0) k_nrc_targets<<<(n + 255) / 256, 256, 0, st>>>(P, C, y, n, clamp_max);
 }
 
-void launch_film(const PathState& P, const WaveDesc& W, float4* film, cudaStream_t st) {
-    k_film<<<(W.npix + 255) / 256, 256, 0, st>>>(P, W, film);
+void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, cudaStream_t st) {
+    k_film<<<(W.npix + 255) / 256, 256, 0, st>>>(P, W, film, imgw);
 }
 
 void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st) {

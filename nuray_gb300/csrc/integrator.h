@@ -12,6 +12,7 @@ struct WaveDesc {
     int32_t npix;
     uint32_t sample0;
     const int32_t* pix_xy;  // device (x, y) list, or null for the full frame
+    int32_t tiled;          // full frame in 8x4 pixel tiles (frame_pixel)
 };
 
 void launch_setup(int num_sms);
@@ -23,7 +24,7 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
 void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int n, cudaStream_t st);
 void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, int n, float clamp_max, cudaStream_t st);
 void launch_reset_counters(uint32_t* counters, cudaStream_t st);
-void launch_film(const PathState& P, const WaveDesc& W, float4* film, cudaStream_t st);
+void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, cudaStream_t st);
 void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st);
 void launch_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8, cudaStream_t st);
 void launch_intersect(const DeviceScene& S, int n, const float* o, const float* d, int* tri, float* t, float* b1,

@@ -349,9 +349,12 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
 
 // Adam on the FP32 master parameters (Kingma & Ba), refreshing the BF16 copy
 // and clearing the gradient.
+// Also advances the moving average used for inference: ema = beta ema +
+// (1 - beta) p, read with the start-up correction 1 / (1 - beta^t).
 __global__ void k_nrc_adam(float* __restrict__ p, float* __restrict__ grad, float* __restrict__ m, float* __restrict__ v,
-                           __nv_bfloat16* __restrict__ wb, int n, float lr, float b1, float b2, float eps, float c1,
-                           float c2) {
+                           __nv_bfloat16* __restrict__ wb, float* __restrict__ ema, float* __restrict__ pinf,
+                           __nv_bfloat16* __restrict__ wb_inf, int n, float lr, float b1, float b2, float eps, float c1,
+                           float c2, float beta, float cema) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float gr = grad[i];
@@ -363,6 +366,11 @@ __global__ void k_nrc_adam(float* __restrict__ p, float* __restrict__ grad, floa
     p[i] = pi;
     wb[i] = __float2bfloat16(pi);
     grad[i] = 0.f;
+    float e = beta * ema[i] + (1.f - beta) * pi;
+    ema[i] = e;
+    float q = beta > 0.f ? e / cema : pi;
+    pinf[i] = q;
+    wb_inf[i] = __float2bfloat16(q);
 }
 
 __global__ void k_f32_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, size_t n) {
@@ -409,10 +417,16 @@ void nrc_launch_backward(const NrcDev& N, const __nv_bfloat16* x, const float* o
     }
 }
 
-void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, cudaStream_t st) {
+void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta, cudaStream_t st) {
     float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-    k_nrc_adam<<<(NRC_NUM_PARAMS + 255) / 256, 256, 0, st>>>(N.params, N.grad, N.m, N.v, N.wb, NRC_NUM_PARAMS, lr, b1,
-                                                            b2, eps, c1, c2);
+    float cema = 1.f - powf(ema_beta, (float)step);
+    k_nrc_adam<<<(NRC_NUM_PARAMS + 255) / 256, 256, 0, st>>>(N.params, N.grad, N.m, N.v, N.wb, N.ema, N.pinf, N.wb_inf,
+                                                            NRC_NUM_PARAMS, lr, b1, b2, eps, c1, c2, ema_beta, cema);
+}
+
+void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, int M, float* out, int num_sms, cudaStream_t st) {
+    if (M <= 0) return;
+    k_nrc_forward<<<grid_for((M + 15) / 16, num_sms), 128, nrc_forward_smem(), st>>>(N.wb_inf, N.pinf, x, M, out, nullptr);
 }
 
 void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t st) {

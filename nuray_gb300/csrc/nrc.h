@@ -31,6 +31,11 @@ struct NrcDev {
     float* m;
     float* v;
     __nv_bfloat16* wb;
+    // exponential moving average of the parameters for inference in renders:
+    // ema (running sum), pinf = ema / (1 - beta^t) and its BF16 copy
+    float* ema;
+    float* pinf;
+    __nv_bfloat16* wb_inf;
 };
 
 void nrc_setup();
@@ -42,7 +47,10 @@ void nrc_launch_forward(const NrcDev& N, const __nv_bfloat16* x, int M, float* o
 void nrc_launch_backward(const NrcDev& N, const __nv_bfloat16* x, const float* out, const float* y,
                          const __nv_bfloat16* acts, __nv_bfloat16* dz, int M, float* loss_sum, int num_sms,
                          cudaStream_t st);
-void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, cudaStream_t st);
+// ema_beta 0 keeps pinf / wb_inf equal to the current parameters.
+void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta, cudaStream_t st);
+// Forward with the inference copy (pinf / wb_inf).
+void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, int M, float* out, int num_sms, cudaStream_t st);
 void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t st);
 
 }  // namespace nr

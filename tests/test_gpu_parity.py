@@ -187,6 +187,12 @@ def test_fast_traversal_tests_equal_exact_ones(gpu_lib):
         np.testing.assert_array_equal(a, b)
 
 
+def test_tiled_frame_order_gives_the_same_image(gpu_lib):
+    S = gpu_scene(cornell_scene())
+    params = "renderer=ptnee imgw=64 imgh=48 spp=4 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
+    np.testing.assert_array_equal(S.render(params + " tile=1"), S.render(params + " tile=0"))
+
+
 def test_accumulate_across_calls_equals_one_call(gpu_lib):
     S = gpu_scene(cornell_scene())
     params = "renderer=ptnee imgw=48 imgh=36 spp=4 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
