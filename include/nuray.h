@@ -208,7 +208,9 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
                          float* b2);
 
 /* Renders the image. params uses the reference grammar ("key=value ..."):
- * imgw imgh spp prr mis (reference keys and defaults) plus seed (Philox seed,
+ * renderer (ptnee, the default, or pt: RendererPT, src/renderer/rendererpt.cpp:13-59,
+ * the same estimator without light sampling), imgw imgh spp prr mis
+ * (reference keys and defaults) plus seed (Philox seed,
  * default 0), rrdepth (first vertex where Russian roulette applies, default 0
  * as in the reference), maxdepth (0 = unbounded as in the reference),
  * wave (paths per wavefront batch, default 2^25), trav (0: traversal with

@@ -117,7 +117,7 @@ __device__ f3 replay(const AdjArgs& A, uint32_t key, uint32_t sample, int x, int
         fac = 1.f;
         dfac_da = 0.f;
         prev_m = m;
-        if (mat_nee(type) && S.num_lights > 0) {
+        if (pol.nee && mat_nee(type) && S.num_lights > 0) {
             float r = rng.next();
             int lo = 0, hi = S.num_lights;
             while (lo < hi) {

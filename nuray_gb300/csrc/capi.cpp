@@ -398,6 +398,11 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
     a.pol.trav = c.get_int("trav", 1);
+    // renderer=ptnee (RendererPTLS) or pt (RendererPT, the same estimator without light sampling)
+    const std::string renderer = c.get_str("renderer");
+    if (renderer.empty() || renderer == "ptnee") a.pol.nee = 1;
+    else if (renderer == "pt") a.pol.nee = 0;
+    else throw NrError(NR_ERR_INVALID, "renderer=" + renderer + " is not implemented (ptnee, pt)");
     if (a.pol.trav < 0 || a.pol.trav > 1) throw NrError(NR_ERR_INVALID, "trav must be 0 or 1");
     a.wave = c.get_int("wave", 1 << 25);
     a.profile = c.get_int("profile", 0) != 0;

@@ -6,8 +6,8 @@
 // e.g. nuray scenes/cornell/CornellBox-Original.obj -s 100 --output result.bmp
 //            --params renderer=ptnee imgw=320 imgh=240 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333
 //
-// renderer must be ptnee (the reference also selects pt/bdpt/pm/pssmlt/nrc;
-// those are not implemented here and are rejected). envmap= (PFM or binary
+// renderer must be ptnee or pt (the reference also selects bdpt, pm, pssmlt
+// and nrc; those are not implemented here and are rejected). envmap= (PFM or binary
 // PPM) and envmap_gain= attach an environment map as the reference CLI does.
 // The output is written as BMP (24-bit, what QImage::save produces for an
 // RGB888 image), PPM (8-bit) or PFM (the linear HDR mean), by extension.
@@ -82,8 +82,8 @@ int main(int argc, char** argv) {
     }
     nr::Config cfg(params.str().c_str());
     std::string renderer = cfg.get_str("renderer");  // Config::getValueStr returns "" when absent
-    if (renderer != "ptnee") {
-        std::cerr << "renderer=" << renderer << " is not available (this build implements renderer=ptnee)\n";
+    if (renderer != "ptnee" && renderer != "pt") {
+        std::cerr << "renderer=" << renderer << " is not available (this build implements renderer=ptnee and pt)\n";
         return 2;
     }
     try {

@@ -240,7 +240,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     }
 
     // next-event estimation (rendererptls.cpp:49-78)
-    if (mat_nee(type) && S.num_lights > 0) {
+    if (pol.nee && mat_nee(type) && S.num_lights > 0) {
         float r = rng.next();
         // LightSampler::sampleLight: lower_bound over the CDF
         int lo = 0, hi = S.num_lights;

@@ -64,6 +64,7 @@ struct Policy {
     int32_t maxdepth; // 0 = unbounded (reference)
     uint32_t seed_lo, seed_hi;
     int32_t imgw, imgh;
+    int32_t nee;      // 1: ptnee (RendererPTLS); 0: pt (RendererPT), no light sampling
     int32_t trav;     // traversal tests: 0 exact arithmetic only, 1 fast path with exact fallback (same hits)
 };
 

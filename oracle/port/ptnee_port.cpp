@@ -570,6 +570,7 @@ struct Scene {
 };
 
 struct Policy {
+    bool nee = true;   // false: RendererPT (src/renderer/rendererpt.cpp:13-59), no light sampling
     float prr = 0.8f;
     bool mis = true;
     int rrdepth = 0;   // RR applies from this vertex index on (0: every vertex, as the reference)
@@ -600,7 +601,7 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
     V3 hit_pos = orig + dir * hit.t;
     V3 result;
     float fac = 1.0f;
-    if (mat_nee(M)) {
+    if (P.nee && mat_nee(M)) {
         int li = S.lights.pick(smp);
         if (li >= 0) {
             const Tri& LT = S.tris[li];
@@ -758,6 +759,10 @@ void port_render_samples(void* s, const char* params, int npix, const int* pix_x
     P.mis = c.i("mis", 1) != 0;
     P.rrdepth = c.i("rrdepth", 0);
     P.maxdepth = c.i("maxdepth", 0);
+    {
+        auto it = c.mp.find("renderer");
+        P.nee = !(it != c.mp.end() && it->second == "pt");
+    }
     int w = c.i("imgw", 1), h = c.i("imgh", 1);
     int nth = threads < 1 ? 1 : threads;
     std::vector<Counters> C(nth);

@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY. This file is compiled together with the
 // unmodified reference sources (src/renderer/rendererptls.cpp,
-// src/renderer/renderer.cpp, src/hierarchy/*.cpp, src/material/*.cpp,
+// src/renderer/rendererpt.cpp, src/renderer/renderer.cpp, src/hierarchy/*.cpp, src/material/*.cpp,
 // src/scene/*.cpp, src/sampler/*.cpp, src/math/vec3.cpp,
 // src/utils/config.cpp) into oracle/_ref/libnuray_ref.so by oracle/Makefile.
 // Only the tests and the golden-fixture script load it; nothing in the
@@ -13,13 +13,15 @@
 //    OBJ/MTL) or from flat arrays (procedural scenes), followed by the
 //    reference's Renderer::prepare (src/renderer/renderer.cpp:30-39);
 //  * the reference BVH query Renderer::intersect (src/renderer/renderer.cpp:10-28);
-//  * the reference estimator RendererPTLS::trace (src/renderer/rendererptls.cpp:13-94)
+//  * the reference estimators RendererPTLS::trace (src/renderer/rendererptls.cpp:13-94)
+//    and, for renderer=pt, RendererPT::trace (src/renderer/rendererpt.cpp:13-59),
 //    driven by the per-pixel sample loop of RendererPTLS::render
 //    (src/renderer/rendererptls.cpp:165-175), with the glibc rand() sampler
 //    replaced by a counter-based Philox stream keyed by (pixel, sample);
 //  * the reference BVH tree, exported in depth-first order;
 //  * the reference Material virtuals on caller-given directions.
 #include "../renderer/rendererptls.h"
+#include "../renderer/rendererpt.h"
 #include "../scene/loader.h"
 #include "../material/matlambert.h"
 #include "../material/matggxrefl.h"
@@ -51,6 +53,13 @@ public:
     float random() override { return i < n ? u[i++] : 0.5f; }
 };
 
+// RendererPT::trace (src/renderer/rendererpt.cpp:13-59), the plain path
+// tracer, driven with the ptnee renderer's BVH and light sampler.
+class OraclePT : public RendererPT {
+public:
+    using RendererPT::trace;
+};
+
 class OracleRenderer : public RendererPTLS {
 public:
     using RendererPTLS::trace;
@@ -70,6 +79,7 @@ struct RefScene {
     std::vector<const Material*> mats;          // first-appearance order
     std::vector<int> tri_mat;                   // per triangle index into mats
     OracleRenderer renderer;
+    OraclePT plain;
     Texture* env_tex = nullptr;
     Envmap* env = nullptr;
     ~RefScene() {
@@ -292,6 +302,9 @@ void ref_render_samples(void* h, const char* params, int npix, const int* pix_xy
     Config config(params);
     Camera cam = make_camera(config);
     int w = config.getValueInt("imgw", 1), hh = config.getValueInt("imgh", 1);
+    std::streambuf* old = std::cerr.rdbuf(nullptr);  // getValueStr reports missing keys on stderr
+    const bool plain = config.getValueStr("renderer", "ptnee") == "pt";
+    std::cerr.rdbuf(old);
     parallel_for(npix, threads, [&](int p) {
         int x = pix_xy[2 * p], y = pix_xy[2 * p + 1];
         Config local = config;  // getValue* builds stringstreams; keep threads apart
@@ -300,8 +313,10 @@ void ref_render_samples(void* h, const char* params, int npix, const int* pix_xy
             float jx = smp.random();
             float jy = smp.random();
             vec3 ray_dir = cam.generateRay(x + jx, y + jy, w, hh);
-            vec3 L = max(0.0f, s->renderer.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
-                                                 s->renderer.bvh(), true, s->env));
+            vec3 L = plain ? max(0.0f, s->plain.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
+                                                      s->renderer.bvh(), s->env))
+                           : max(0.0f, s->renderer.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
+                                                         s->renderer.bvh(), true, s->env));
             float* o = out + ((size_t)p * spp + i) * 3;
             o[0] = L[0]; o[1] = L[1]; o[2] = L[2];
         }

@@ -126,7 +126,8 @@ def test_samples_mixed_same_stream(gpu_lib):
     assert _sample_match(rad, g["rad"]) >= 0.97
 
 
-@pytest.mark.parametrize("extra", ["rrdepth=3 maxdepth=8", "mis=0 prr=0.6", "maxdepth=2", "seed=12345678901"])
+@pytest.mark.parametrize("extra", ["rrdepth=3 maxdepth=8", "mis=0 prr=0.6", "maxdepth=2", "seed=12345678901",
+                                   "renderer=pt"])
 def test_samples_policies_vs_port(gpu_lib, port_lib, extra):
     sc = cornell_scene()
     S, P = gpu_scene(sc), Oracle("port", sc)

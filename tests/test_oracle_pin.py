@@ -125,6 +125,15 @@ def test_port_equals_reference_mixed(port_lib, ref_lib, seed):
         np.testing.assert_array_equal(a, b)
 
 
+def test_port_equals_reference_plain_pt(port_lib, ref_lib):
+    """renderer=pt: RendererPT::trace (src/renderer/rendererpt.cpp:13-59)."""
+    sc = scenes.small_scene(6)
+    P, R = Oracle("port", sc), Oracle("ref", sc)
+    pix = pixel_grid(48, 32)
+    params = sc["params"].replace("renderer=ptnee", "renderer=pt")
+    np.testing.assert_array_equal(P.render_samples(params, pix, 4, seed=6), R.render_samples(params, pix, 4, seed=6))
+
+
 def test_port_equals_reference_no_lights_and_empty(port_lib, ref_lib):
     sc = scenes.small_scene(4)
     # drop the emitters: NEE then finds no light (LightSampler returns nullptr)
