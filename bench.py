@@ -13,6 +13,8 @@ value: paths / s with the scene resident and the image left on the device
 (nr_render with no host output), timed with CUDA events on the library's
 stream. e2e: the same render through nr_render with a pinned host output
 image, so the 24.9 MB device-to-host copy is inside the timed region.
+time_to_relmse (after the timed steps, not part of `value`): the metric's
+second half, plain PT against PT + the online neural radiance cache.
 
 Multi-GPU (torchrun): every rank renders its own 64-sample range of the
 frame (sample0 = 64 * rank) with no collective on the data path (weak
@@ -60,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-tile-stride", type=int, default=32, help="CPU sample: every k-th 4x4 tile")
+    ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE comparison")
+    ap.add_argument("--relmse-res", default="960x540")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
                     help="c2: the 1M-triangle scene (default); c3: the same with an HDR sky, value-noise "
                          "textures on half the materials and 10%% GGX dielectrics, spp 256")
@@ -172,6 +176,22 @@ def cpu_leg(sc, params, spp, w, h, stride, budget_s=20.0):
     desc = (f"{n} pixels (every {stride}th 4x4 tile, first {n}) x {spp} spp of the same frame, "
             f"{n * spp} paths in {dt:.1f} s")
     return n * spp / dt / 1e6, desc, threads
+
+
+def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0):
+    """Second half of the metric: wall time (CUDA events) to relMSE <= 1e-3
+    against a converged render, plain PT against PT + the online neural
+    radiance cache, both progressive at one sample per pixel per frame."""
+    from nuray_gb300 import convergence as C
+    w, h = res.split("x")
+    p = params.replace("imgw=1920", f"imgw={w}").replace("imgh=1080", f"imgh={h}")
+    ref = C.reference(S, p, ref_spp)
+    pt_curve, pt_t = C.progressive(S, p, 100000, ref, target, time_limit_s=limit_s)
+    nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "nrc_train=16384", limit_s)
+    return {"target": target, "resolution": res, "reference_spp": ref_spp, "unit": "ms",
+            "pt": C.summary(pt_curve, pt_t), "pt_nrc": C.summary(nrc_curve, nrc_t),
+            "note": "GPU time (CUDA events) of the frames up to the first checkpoint at or below the target; "
+                    "None when not reached within the time limit"}
 
 
 def run_reference(args, rank, world):
@@ -329,6 +349,8 @@ def main():
            "e2e": e2e, "clocks": clk.summary()}
     if e2e:
         out["gpu_launches_e2e"] = launches_e2e * args.steps
+    if not args.no_relmse and world == 1:
+        out["time_to_relmse"] = relmse_leg(S, params, args.relmse_res)
     print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -19,11 +19,15 @@ def relmse(img, ref):
     return float(np.mean((a - r) ** 2 / (r ** 2 + 1e-2)))
 
 
-def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", time_limit_s=60.0, growth=1.03):
+def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", time_limit_s=60.0, growth=1.03,
+                warmup=0):
     """Renders up to `frames` 1-spp frames, accumulated on the device; the
     image is read back and compared at checkpoints spaced by `growth` in
-    sample count. Returns (elapsed_ms, spp, relmse) rows and the elapsed GPU
-    time at the first checkpoint that meets `target`."""
+    sample count. With a cache, the first `warmup` frames are plain path
+    tracing that only trains it (unbiased samples that count towards the
+    image); later frames end paths in the cache. Returns (elapsed_ms, spp,
+    relmse) rows and the elapsed GPU time at the first checkpoint that meets
+    `target`."""
     import torch
     stream = torch.cuda.ExternalStream(scene.stream())
     curve = []
@@ -34,7 +38,7 @@ def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", tim
     for k in range(frames):
         p = params.replace("spp=", "spp_unused=") + f" spp=1 sample0={k}" + (" accumulate=1" if k else "")
         if nrc is not None:
-            p += " nrc=1 " + nrc_params
+            p += " nrc=1 " + nrc_params + (" nrc_query=0" if k < warmup else "")
         check = k + 1 >= next_check or k == frames - 1
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -58,14 +62,14 @@ def reference(scene, params, ref_spp=8192, seed_ref=12345):
     return scene.render(params.replace("spp=", "spp_unused=") + f" spp={ref_spp} seed={seed_ref}")
 
 
-def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s):
+def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s, warmup=64):
     from ._lib import check, lib
     from .nrc import Cache
     cache = Cache("lr=1e-3 beta1=0.9 beta2=0.99")
     cache.attach(scene)
     try:
         return progressive(scene, params, frames, ref, target, nrc=cache, nrc_params=nrc_params,
-                           time_limit_s=time_limit_s)
+                           time_limit_s=time_limit_s, warmup=warmup)
     finally:
         check(lib().nr_scene_attach_nrc(scene._h, None))
         cache.close()

@@ -309,7 +309,7 @@ void ensure_paths(nr_scene* s, int cap) {
     if (cap <= s->capacity) return;
     const size_t C = (size_t)cap;
     const size_t f4 = 16;
-    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 2 + C * 4 * nr::NUM_CAT + C * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
+    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 16 + C * 4 * nr::NUM_CAT + C * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
     s->path_mem.alloc(bytes);
     char* p = s->path_mem.as<char>();
     auto take = [&](size_t n) { char* r = p; p += (n + 255) & ~size_t(255); return r; };
@@ -320,8 +320,8 @@ void ensure_paths(nr_scene* s, int cap) {
     P.thr = (float4*)take(C * f4);
     P.rad = (float4*)take(C * f4);
     P.meta = (uint4*)take(C * 16);
-    P.queue_in = (int32_t*)take(C * 4);
-    P.queue_out = (int32_t*)take(C * 4);
+    P.queue_in = (int32_t*)take(C * 4 * 8);
+    P.queue_out = (int32_t*)take(C * 4 * 8);
     P.sorted = (int32_t*)take(C * 4 * nr::NUM_CAT);
     P.sh_o = (float4*)take(C * f4);
     P.sh_d = (float4*)take(C * f4);
@@ -398,6 +398,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
     a.pol.trav = c.get_int("trav", 1);
+    a.pol.sortdir = c.get_int("sortdir", 1) != 0 ? 1 : 0;
     // renderer=ptnee (RendererPTLS) or pt (RendererPT, the same estimator without light sampling)
     const std::string renderer = c.get_str("renderer");
     if (renderer.empty() || renderer == "ptnee") a.pol.nee = 1;

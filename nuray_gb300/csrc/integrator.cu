@@ -79,7 +79,10 @@ __global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, P
     P.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P.meta[i] = make_uint4(key, sample, s.n, 0u);
     P.queue_in[i] = i;
-    if (i == 0) P.counters[CNT_IN] = (uint32_t)W.count;
+    if (i == 0) {
+        P.counters[CNT_IN] = (uint32_t)W.count;
+        P.counters[CNT_DIR_IN] = (uint32_t)W.count;  // octant bucket 0 holds the camera rays in frame order
+    }
 }
 
 // ---------------------------------------------------------------- closest hit + sort
@@ -106,6 +109,10 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
     const uint32_t n = P.counters[CNT_IN];
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
+    uint32_t start[9];
+    start[0] = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) start[k + 1] = start[k] + P.counters[CNT_DIR_IN + k];
     while (true) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK], 32u);
@@ -113,7 +120,10 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
         if (base >= n) break;
         uint32_t idx = base + lane;
         if (idx < n) {
-            int slot = P.queue_in[idx];
+            int oct = 0;
+#pragma unroll
+            for (int k = 1; k < 8; ++k) if (idx >= start[k]) oct = k;
+            int slot = P.queue_in[(size_t)oct * capacity + (idx - start[oct])];
             f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
             float t, b1, b2;
             int tri = closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
@@ -172,7 +182,7 @@ __device__ __forceinline__ bool nrc_is_training(uint32_t pixel, uint32_t sample,
 
 template <bool NRC>
 __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
-                                          const NrcCtx& C) {
+                                          const NrcCtx& C, int capacity) {
     float4 h = P.hit[slot];
     float4 thr = P.thr[slot];
     uint4 meta = P.meta[slot];
@@ -301,8 +311,9 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     // contri = Li * |wi.n| * brdf / pdf / prr (rendererptls.cpp:90)
     f3 Tn = T * fabsf(dot(wi, normal)) * brdf / pdf / prr;
     f3 no = hit_pos + wi * 1e-3f;
-    int q = warp_append(true, &P.counters[CNT_OUT]);
-    P.queue_out[q] = slot;
+    const int oct = pol.sortdir ? ((wi.x < 0.f ? 1 : 0) | (wi.y < 0.f ? 2 : 0) | (wi.z < 0.f ? 4 : 0)) : 0;
+    int q = warp_append_keyed(oct, &P.counters[CNT_DIR_OUT]);
+    P.queue_out[(size_t)oct * capacity + q] = slot;
     P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
     P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
     P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
@@ -322,7 +333,7 @@ __global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Polic
 #pragma unroll
         for (int k = 1; k < NUM_CAT; ++k) if (i >= start[k]) c = k;
         int slot = P.sorted[(size_t)c * capacity + (i - start[c])];
-        shade_one<NRC>(P, S, pol, slot, C);
+        shade_one<NRC>(P, S, pol, slot, C, capacity);
     }
 }
 
@@ -335,7 +346,13 @@ __global__ void k_advance(uint32_t* counters) {
     unsigned long long* shr = reinterpret_cast<unsigned long long*>(counters + CNT_SHRAYS);
     *rays += in;
     *shr += sh;
-    counters[CNT_IN] = counters[CNT_OUT];
+    uint32_t live = 0;
+    for (int k = 0; k < 8; ++k) {
+        live += counters[CNT_DIR_OUT + k];
+        counters[CNT_DIR_IN + k] = counters[CNT_DIR_OUT + k];
+        counters[CNT_DIR_OUT + k] = 0;
+    }
+    counters[CNT_IN] = live;
     counters[CNT_OUT] = 0;
     counters[CNT_SHADOW] = 0;
     counters[CNT_WORK] = 0;
@@ -347,7 +364,7 @@ __global__ void k_advance(uint32_t* counters) {
 // CNT_RAYS on are kept for the whole render.
 __global__ void k_reset_counters(uint32_t* counters) {
     int i = threadIdx.x;
-    if (i < CNT_RAYS && i != CNT_ERR) counters[i] = 0;
+    if ((i < CNT_RAYS && i != CNT_ERR) || (i >= CNT_DIR_IN && i < NUM_COUNTERS)) counters[i] = 0;
 }
 
 // ---------------------------------------------------------------- film
@@ -502,7 +519,7 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
     k_advance<<<1, 1, 0, st>>>(P.counters);
 }
 
-void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, 32, 0, st>>>(counters); }
+void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, NUM_COUNTERS, 0, st>>>(counters); }
 
 void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int n, cudaStream_t st) {
     if (n > 0) k_nrc_apply<<<(n + 255) / 256, 256, 0, st>>>(P, C, pred, n);

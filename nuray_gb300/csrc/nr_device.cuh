@@ -110,12 +110,17 @@ struct SlabRay {
     float ox, oy, oz;
     float dx, dy, dz;     // d + 1e-9f
     float rx, ry, rz;     // RN(1 / (d + 1e-9f))
+    float cx, cy, cz;     // RN(-o * r), for the one-FMA approximate quotient
+    float abs_err;        // bound on |fma(b, r, c) - (b - o) r| from rounding c
 };
 __device__ __forceinline__ SlabRay make_slab_ray(f3 o, f3 d) {
     SlabRay r;
     r.ox = o.x; r.oy = o.y; r.oz = o.z;
     r.dx = __fadd_rn(d.x, 1e-9f); r.dy = __fadd_rn(d.y, 1e-9f); r.dz = __fadd_rn(d.z, 1e-9f);
     r.rx = __frcp_rn(r.dx); r.ry = __frcp_rn(r.dy); r.rz = __frcp_rn(r.dz);
+    r.cx = -o.x * r.rx; r.cy = -o.y * r.ry; r.cz = -o.z * r.rz;
+    // |c| * 2^-24 (rounding of c) with headroom: 2^-22
+    r.abs_err = 2.4e-7f * fmaxf(fabsf(r.cx), fmaxf(fabsf(r.cy), fabsf(r.cz)));
     return r;
 }
 
@@ -146,14 +151,16 @@ __device__ __forceinline__ bool box_test(const SlabRay& r, float lx, float hx, f
 // within that error of each other; those cases are recomputed exactly.
 __device__ __forceinline__ bool box_test_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
                                               float& t_entry) {
-    float x1 = __fmul_rn(__fsub_rn(lx, r.ox), r.rx), x2 = __fmul_rn(__fsub_rn(hx, r.ox), r.rx);
-    float y1 = __fmul_rn(__fsub_rn(ly, r.oy), r.ry), y2 = __fmul_rn(__fsub_rn(hy, r.oy), r.ry);
-    float z1 = __fmul_rn(__fsub_rn(lz, r.oz), r.rz), z2 = __fmul_rn(__fsub_rn(hz, r.oz), r.rz);
+    // one FMA per bound: fma(b, r, -o r) is within 2^-22.4 |q| + abs_err of
+    // the exact quotient q = (b - o) / d
+    float x1 = __fmaf_rn(lx, r.rx, r.cx), x2 = __fmaf_rn(hx, r.rx, r.cx);
+    float y1 = __fmaf_rn(ly, r.ry, r.cy), y2 = __fmaf_rn(hy, r.ry, r.cy);
+    float z1 = __fmaf_rn(lz, r.rz, r.cz), z2 = __fmaf_rn(hz, r.rz, r.cz);
     float tin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fmaxf(fminf(z1, z2), -1e18f));
     float tout = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fminf(fmaxf(z1, z2), 1e18f));
-    float margin = 1e-6f * fmaxf(fabsf(tin), fabsf(tout));  // about 8x the quotient error
-    if (tout < 0.0f) return false;  // exact: the signs of the quotients are exact
-    if (tin + margin < tout) { t_entry = tin; return true; }
+    float margin = 1e-6f * fmaxf(fabsf(tin), fabsf(tout)) + r.abs_err;
+    if (tout < -margin) return false;
+    if (tin + margin < tout && tout > margin) { t_entry = tin; return true; }
     if (tin > tout + margin) return false;
     return box_test(r, lx, hx, ly, hy, lz, hz, t_entry);
 }
