@@ -61,13 +61,19 @@ def parse():
     ap.add_argument("--wave", type=int, default=0, help="paths per wavefront batch (0: library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--cpu-tile-stride", type=int, default=32, help="CPU sample: every k-th 4x4 tile")
+    ap.add_argument("--cpu-tile-stride", type=int, default=4, help="CPU sample: every k-th 4x4 tile")
     ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE comparison")
     ap.add_argument("--relmse-res", default="960x540")
+    ap.add_argument("--nrc", default=None, metavar="PARAMS",
+                    help="each step is a PT + NRC frame: a fresh cache is attached and the render gets "
+                         "'nrc=1 nrc_train=16384 PARAMS' (measures the cache's per-frame cost)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
                     help="c2: the 1M-triangle scene (default); c3: the same with an HDR sky, value-noise "
                          "textures on half the materials and 10%% GGX dielectrics, spp 256")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.nrc is not None:
+        args.no_relmse = True  # the comparison attaches caches of its own
+    return args
 
 
 def dist_env():
@@ -244,8 +250,15 @@ def main():
                           env_tex=sc["env_tex"], env_gain=sc["env_gain"])
     build_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(S.stream())
-    spp = args.spp
-    base = params + f" sample0={spp * rank}"
+    cache = None
+    if args.nrc is not None:
+        from nuray_gb300.nrc import Cache
+        cache = Cache("lr=1e-3 beta1=0.9 beta2=0.99")
+        cache.attach(S)
+        params += " nrc=1 nrc_train=16384 " + args.nrc
+    from nuray_gb300.shard import max_over_ranks, sample_range
+    sample0, spp = sample_range(rank, world, args.spp, "weak")
+    base = params + f" sample0={sample0}"
 
     # untimed instrumented frame: traversal work per ray for the roofline bytes
     S.render_device(base.replace(f"spp={spp}", "spp=1") + " count=1")
@@ -274,11 +287,7 @@ def main():
         ev1.record(stream)
         ev1.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     paths_total = float(w * h * spp * args.steps * world)
     value = paths_total / (ms / 1e3) / 1e6
 
@@ -297,11 +306,7 @@ def main():
         e1.record(stream)
         e1.synchronize()
         barrier()
-        ems = e0.elapsed_time(e1)
-        if dist is not None:
-            t2 = torch.tensor([ems], device="cuda")
-            dist.all_reduce(t2, op=dist.ReduceOp.MAX)
-            ems = float(t2.item())
+        ems = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
         e2e = {"value": round(paths_total / (ems / 1e3) / 1e6, 3), "unit": "Mpaths/s",
                "h2d_bytes_per_step": len(base.encode()) + 44, "d2h_bytes_per_step": w * h * 3 * 4,
                "ms_per_step": round(ems / args.steps, 2)}
@@ -336,7 +341,7 @@ def main():
         v, sample, threads = cpu_leg(sc, params, spp, w, h, args.cpu_tile_stride)
         cpu = {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": sample}
 
-    out = {"metric": "Mpaths/s ptnee", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world,
+    out = {"metric": "Mpaths/s ptnee" + ("+nrc" if cache else ""), "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 2),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded procedural scene; the reference publishes no benchmark scene)",

@@ -115,7 +115,6 @@ typedef struct nr_camera {
 
 typedef struct nr_scene nr_scene;
 
-/* Render statistics of the last nr_render / nr_render_samples on a scene. */
 /* Render statistics of the last nr_render / nr_render_samples on a scene.
  * Kernel times are filled when the parameters contain profile=1 (CUDA events
  * around every kernel of the wavefront), traversal counts when they contain
@@ -219,7 +218,10 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * the previous call of the same size instead of clearing it; the outputs are
  * the mean over all samples added so far), sample0 (index of the first
  * sample, default 0: renders of disjoint sample ranges are independent and
- * their films sum), profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
+ * their films sum), tile (1, the default: the paths of a wave are ordered by
+ * 8x4 pixel tiles when imgw % 8 == 0 and imgh % 4 == 0, so a warp's camera
+ * rays are coherent; 0: scanline order; the image is the same either way),
+ * profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
  * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
  * (W*H*3 bytes: mean^(1/2.2)*255 clamped and truncated, as
  * src/renderer/rendererptls.cpp:175-180) may each be NULL. cancel, if not
@@ -279,8 +281,17 @@ int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, fl
  * vertex depth >= nrc_mindepth (default 1), with the cache's prediction, and
  * trains the cache online on the suffix radiance of nrc_train (default
  * 16384) training paths per wavefront batch in nrc_steps (default 4) Adam
- * steps; nrc_query=0 only trains. NULL detaches. The cache must not be used
- * through nr_nrc_* while a render of the scene runs. */
+ * steps. Training paths end in the cache too, from vertex depth
+ * nrc_train_depth on (default 3; 0 lets them run to the end), as the
+ * reference's path_lim_train does (src/renderer/renderernrc.cpp:130). The
+ * counts stay on the device: a render with nrc=1 adds no host
+ * synchronisation. nrc_query=0 only trains. With nrc_direct=1 (default) the
+ * query vertex still takes its light sample (shadow ray) and the cache
+ * stands in only for the radiance after it; nrc_direct=0 makes the cache
+ * stand in for all of it. A cache trained one way must be queried the same
+ * way.
+ * NULL detaches. The cache must not be used through nr_nrc_* while a render
+ * of the scene runs. */
 int nr_scene_attach_nrc(nr_scene* scene, nr_nrc* nrc);
 
 /* ------------------------------------------------------------------------

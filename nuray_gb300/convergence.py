@@ -62,7 +62,7 @@ def reference(scene, params, ref_spp=8192, seed_ref=12345):
     return scene.render(params.replace("spp=", "spp_unused=") + f" spp={ref_spp} seed={seed_ref}")
 
 
-def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s, warmup=64):
+def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s, warmup=256):
     from ._lib import check, lib
     from .nrc import Cache
     cache = Cache("lr=1e-3 beta1=0.9 beta2=0.99")

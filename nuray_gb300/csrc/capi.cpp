@@ -309,7 +309,7 @@ void ensure_paths(nr_scene* s, int cap) {
     if (cap <= s->capacity) return;
     const size_t C = (size_t)cap;
     const size_t f4 = 16;
-    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 16 + C * 4 * nr::NUM_CAT + C * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
+    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 2 + C * 4 * nr::NUM_CAT + C * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
     s->path_mem.alloc(bytes);
     char* p = s->path_mem.as<char>();
     auto take = [&](size_t n) { char* r = p; p += (n + 255) & ~size_t(255); return r; };
@@ -320,8 +320,8 @@ void ensure_paths(nr_scene* s, int cap) {
     P.thr = (float4*)take(C * f4);
     P.rad = (float4*)take(C * f4);
     P.meta = (uint4*)take(C * 16);
-    P.queue_in = (int32_t*)take(C * 4 * 8);
-    P.queue_out = (int32_t*)take(C * 4 * 8);
+    P.queue_in = (int32_t*)take(C * 4);
+    P.queue_out = (int32_t*)take(C * 4);
     P.sorted = (int32_t*)take(C * 4 * nr::NUM_CAT);
     P.sh_o = (float4*)take(C * f4);
     P.sh_d = (float4*)take(C * f4);
@@ -356,11 +356,12 @@ void nrc_ensure_batch(nr_nrc* c, int m) {
 void nrc_train_device(nr_nrc* c, const __nv_bfloat16* x, const float* y, int m, bool update, cudaStream_t st) {
     nrc_ensure_batch(c, m);
     NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
-    nr::nrc_launch_forward(c->dev, x, m, c->out, c->acts, c->num_sms, st);
-    nr::nrc_launch_backward(c->dev, x, c->out, y, c->acts, c->dz, m, c->loss, c->num_sms, st);
+    const nr::NrcRows R = nr::nrc_rows(m);
+    nr::nrc_launch_forward(c->dev, x, R, c->out, c->acts, c->num_sms, st);
+    nr::nrc_launch_backward(c->dev, x, c->out, y, c->acts, c->dz, R, c->loss, c->num_sms, st);
     if (update) {
         c->step++;
-        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, st);
+        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st);
     }
 }
 
@@ -380,6 +381,8 @@ struct RenderArgs {
     int nrc_query;    // 0: train only
     int nrc_mindepth; // first vertex at which a path may end in the cache
     float nrc_rough;  // roughness from which a GGX vertex is diffuse
+    int nrc_direct;   // 1: light sample at the query vertex, cache for the rest
+    int nrc_train_depth;  // > 0: training paths end in the cache from this depth on
 };
 
 RenderArgs parse_args(const nr_camera* cam, const char* params) {
@@ -398,7 +401,6 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
     a.pol.trav = c.get_int("trav", 1);
-    a.pol.sortdir = c.get_int("sortdir", 1) != 0 ? 1 : 0;
     // renderer=ptnee (RendererPTLS) or pt (RendererPT, the same estimator without light sampling)
     const std::string renderer = c.get_str("renderer");
     if (renderer.empty() || renderer == "ptnee") a.pol.nee = 1;
@@ -417,6 +419,9 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.nrc_query = c.get_int("nrc_query", 1);
     a.nrc_mindepth = c.get_int("nrc_mindepth", 1);
     a.nrc_rough = c.get_float("nrc_rough", 0.2f);
+    a.nrc_direct = c.get_int("nrc_direct", 1) != 0 ? 1 : 0;
+    a.nrc_train_depth = c.get_int("nrc_train_depth", 3);
+    if (a.nrc_train_depth < 0) throw NrError(NR_ERR_INVALID, "nrc_train_depth must be >= 0");
     if (a.nrc && (a.nrc_train <= 0 || a.nrc_steps <= 0)) throw NrError(NR_ERR_INVALID, "nrc_train and nrc_steps must be positive");
     if (a.sample0 < 0) throw NrError(NR_ERR_INVALID, "sample0 must be >= 0");
     if (a.pol.imgw <= 0 || a.pol.imgh <= 0) throw NrError(NR_ERR_INVALID, "imgw and imgh must be positive");
@@ -468,6 +473,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         X.query = A.nrc_query;
         X.min_depth = A.nrc_mindepth;
         X.rough = A.nrc_rough;
+        X.direct = A.nrc_direct;
+        X.train_depth = A.nrc_train_depth;
         for (int k = 0; k < 3; ++k) {
             float ext = s->dev.root_hi[k] - s->dev.root_lo[k];
             X.lo[k] = s->dev.root_lo[k];
@@ -477,6 +484,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     }
     const float film_h = nr::film_height(A.cam);
     auto t0 = std::chrono::steady_clock::now();
+    int nrc_loss_pending = 0;  // training steps behind the loss copied to the cache's pinned buffer
     nr_stats& S = s->stats;
     S = nr_stats{};
     // profile=1: events are recorded in sequence and read once at the end,
@@ -542,41 +550,28 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             }
         }
         if (use_nrc) {
-            // cache queries of this batch, then training on its training paths
-            uint32_t qt[2];
-            NR_CUDA(cudaMemcpyAsync(s->counters_host, s->nrc_ctx.counters, 8, cudaMemcpyDeviceToHost, st));
-            NR_CUDA(cudaStreamSynchronize(st));
-            qt[0] = s->counters_host[0];
-            qt[1] = std::min<uint32_t>(s->counters_host[1], (uint32_t)s->nrc_tcap);
+            // Cache queries of this batch, then training on its training
+            // paths. The query and record counts stay on the device: every
+            // launch reads them there, so the host never waits here.
             nr_nrc* c = s->nrc;
-            if (qt[0] > 0) {
-                nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)s->nrc_ctx.q_x, (int)qt[0], s->nrc_pred,
-                                           c->num_sms, st);
-                nr::launch_nrc_apply(s->ps, s->nrc_ctx, s->nrc_pred, (int)qt[0], st);
-                S.kernel_launches += 2;
+            const nr::NrcCtx& X = s->nrc_ctx;
+            nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)X.q_x, nr::nrc_rows_counted(&X.counters[0], cap, 0, 1),
+                                       s->nrc_pred, c->num_sms, st);
+            nr::launch_nrc_apply(s->ps, X, s->nrc_pred, cap, st);
+            nr::launch_nrc_targets(s->ps, X, c->y, 1e3f, st);
+            NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
+            const int steps = A.nrc_steps;
+            for (int k = 0; k < steps; ++k) {
+                const nr::NrcRows R = nr::nrc_rows_counted(&X.counters[1], s->nrc_tcap, k, steps);
+                const __nv_bfloat16* x = (const __nv_bfloat16*)X.t_x;
+                nr::nrc_launch_forward(c->dev, x, R, c->out, c->acts, c->num_sms, st);
+                nr::nrc_launch_backward(c->dev, x, c->out, c->y, c->acts, c->dz, R, c->loss, c->num_sms, st);
+                c->step++;
+                nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st);
             }
-            if (qt[1] > 0) {
-                nr::launch_nrc_targets(s->ps, s->nrc_ctx, c->y, (int)qt[1], 1e3f, st);
-                const int steps = std::min<int>(A.nrc_steps, (int)qt[1]);
-                const int chunk = ((int)qt[1] + steps - 1) / steps;
-                for (int k = 0; k < steps; ++k) {
-                    int m0 = k * chunk, m = std::min<int>(chunk, (int)qt[1] - m0);
-                    if (m <= 0) break;
-                    const __nv_bfloat16* x = (const __nv_bfloat16*)s->nrc_ctx.t_x + (size_t)m0 * NRC_IN;
-                    // y of the chunk lives at c->y + 3 m0; the batch scratch is sized for all records
-                    nr::nrc_launch_forward(c->dev, x, m, c->out, c->acts, c->num_sms, st);
-                    NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
-                    nr::nrc_launch_backward(c->dev, x, c->out, c->y + 3 * (size_t)m0, c->acts, c->dz, m, c->loss,
-                                            c->num_sms, st);
-                    c->step++;
-                    nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, st);
-                    S.kernel_launches += 9;
-                }
-                NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, st));
-                NR_CUDA(cudaStreamSynchronize(st));
-                s->nrc_last_loss = *c->loss_host / (3.0f * (float)chunk);
-                S.kernel_launches += 1;
-            }
+            NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, st));
+            nrc_loss_pending = steps;
+            S.kernel_launches += 3 + 4 * steps;
         }
         mark(-1);
         if (film) nr::launch_film(s->ps, W, film, A.pol.imgw, st);
@@ -592,6 +587,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters, nr::NUM_COUNTERS * 4, cudaMemcpyDeviceToHost, st));
     NR_CUDA(cudaStreamSynchronize(st));
     NR_CUDA(cudaGetLastError());
+    if (nrc_loss_pending) s->nrc_last_loss = *s->nrc->loss_host / (float)nrc_loss_pending;
     uint32_t* c = s->counters_host;
     auto u64 = [&](int i) { return (uint64_t)c[i] | ((uint64_t)c[i + 1] << 32); };
     S.paths = total;
@@ -1015,7 +1011,7 @@ int nr_nrc_infer(nr_nrc* c, int32_t n, const float* x, float* out) {
         std::lock_guard<std::mutex> lk(c->mu);
         NR_CUDA(cudaSetDevice(c->device));
         nrc_upload_x(c, n, x);
-        nr::nrc_launch_forward(c->dev, c->x, n, c->out, nullptr, c->num_sms, c->stream);
+        nr::nrc_launch_forward(c->dev, c->x, nr::nrc_rows(n), c->out, nullptr, c->num_sms, c->stream);
         NR_CUDA(cudaMemcpyAsync(out, c->out, (size_t)n * 12, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaStreamSynchronize(c->stream));
         NR_CUDA(cudaGetLastError());
@@ -1033,14 +1029,14 @@ static int nrc_grad_impl(nr_nrc* c, int32_t n, const float* x, const float* y, f
         if (grad) NR_CUDA(cudaMemcpyAsync(grad, c->dev.grad, NRC_NUM_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream));
         if (update) {
             c->step++;
-            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, c->stream);
+            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, nr::nrc_rows(n), c->stream);
         } else {
             NR_CUDA(cudaMemsetAsync(c->dev.grad, 0, NRC_NUM_PARAMS * 4, c->stream));
         }
         NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaStreamSynchronize(c->stream));
         NR_CUDA(cudaGetLastError());
-        if (loss) *loss = *c->loss_host / (3.0f * (float)n);
+        if (loss) *loss = *c->loss_host;
     });
 }
 

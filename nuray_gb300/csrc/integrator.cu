@@ -79,10 +79,7 @@ __global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, P
     P.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P.meta[i] = make_uint4(key, sample, s.n, 0u);
     P.queue_in[i] = i;
-    if (i == 0) {
-        P.counters[CNT_IN] = (uint32_t)W.count;
-        P.counters[CNT_DIR_IN] = (uint32_t)W.count;  // octant bucket 0 holds the camera rays in frame order
-    }
+    if (i == 0) P.counters[CNT_IN] = (uint32_t)W.count;
 }
 
 // ---------------------------------------------------------------- closest hit + sort
@@ -109,10 +106,6 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
     const uint32_t n = P.counters[CNT_IN];
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
-    uint32_t start[9];
-    start[0] = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) start[k + 1] = start[k] + P.counters[CNT_DIR_IN + k];
     while (true) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK], 32u);
@@ -120,10 +113,7 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
         if (base >= n) break;
         uint32_t idx = base + lane;
         if (idx < n) {
-            int oct = 0;
-#pragma unroll
-            for (int k = 1; k < 8; ++k) if (idx >= start[k]) oct = k;
-            int slot = P.queue_in[(size_t)oct * capacity + (idx - start[oct])];
+            int slot = P.queue_in[idx];
             f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
             float t, b1, b2;
             int tri = closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
@@ -144,7 +134,7 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
 // Shadow rays, persistent like k_trace: occluded when any reachable triangle
 // has t <= the ray's limit (any_hit); unoccluded rays add their NEE term.
 template <bool COUNT, bool FAST>
-__global__ void __launch_bounds__(128) k_shadow(PathState P, DeviceScene S) {
+__global__ void __launch_bounds__(128) k_shadow(PathState P, DeviceScene S, float4* t_before) {
     const uint32_t n = P.counters[CNT_SHADOW];
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
@@ -161,6 +151,12 @@ __global__ void __launch_bounds__(128) k_shadow(PathState P, DeviceScene S) {
                 float4 c = P.sh_c[idx];
                 float4 r = P.rad[slot];
                 P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+                // a cache training record that excludes its vertex's light sample
+                const int rec = __float_as_int(c.w);
+                if (t_before && rec >= 0) {
+                    float4 b = t_before[rec];
+                    t_before[rec] = make_float4(b.x + c.x, b.y + c.y, b.z + c.z, 0.f);
+                }
             }
         }
     }
@@ -182,7 +178,7 @@ __device__ __forceinline__ bool nrc_is_training(uint32_t pixel, uint32_t sample,
 
 template <bool NRC>
 __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
-                                          const NrcCtx& C, int capacity) {
+                                          const NrcCtx& C) {
     float4 h = P.hit[slot];
     float4 thr = P.thr[slot];
     uint4 meta = P.meta[slot];
@@ -225,18 +221,23 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     float fac = 1.0f;
     const int depth = (int)(meta.w & NR_META_DEPTH_MASK);
     uint32_t flags = meta.w & NR_META_SEEN_DIFFUSE;
+    bool query_here = false;
+    int rec = -1;  // training record whose target leaves out this vertex's light sample
     if (NRC) {
         const bool train = nrc_is_training(meta.x, meta.y, C.train_stride);
-        if (!train && flags && C.query && depth >= C.min_depth) {
-            // past the first diffuse bounce: the cache stands in for the rest of the path
+        // Past the first diffuse bounce the cache stands in for the rest of the
+        // path: from depth min_depth on, or for training paths from
+        // train_depth on (their earlier vertices then learn from it).
+        const bool end_here = train ? (C.train_depth > 0 && depth >= C.train_depth) : depth >= C.min_depth;
+        if (flags && C.query && end_here) {
             int q = warp_append(true, &C.counters[0]);
             C.q_slot[q] = slot;
             C.q_thr[q] = make_float4(T.x, T.y, T.z, 0.f);
             nrc_encode(reinterpret_cast<uint32_t*>(C.q_x) + (size_t)q * 40, C.lo, C.inv_ext, hit_pos, wo, normal,
                        nrc_roughness(M), M.c0);
-            return;
-        }
-        if (train) {
+            if (!C.direct) return;
+            query_here = true;  // the light sample below stays explicit
+        } else if (train) {
             int r = warp_append(true, &C.counters[1]);
             if (r < C.tcap) {
                 C.t_slot[r] = slot;
@@ -244,6 +245,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
                 C.t_before[r] = P.rad[slot];
                 nrc_encode(reinterpret_cast<uint32_t*>(C.t_x) + (size_t)r * 40, C.lo, C.inv_ext, hit_pos, wo, normal,
                            nrc_roughness(M), M.c0);
+                if (C.direct) rec = r;
             }
         }
         if (nrc_diffuse(M, C.rough)) flags = NR_META_SEEN_DIFFUSE;
@@ -293,13 +295,18 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
                 f3 so = hit_pos + wl * 1e-3f;
                 P.sh_o[q] = make_float4(so.x, so.y, so.z, tmax);
                 P.sh_d[q] = make_float4(wl.x, wl.y, wl.z, __int_as_float(slot));
-                P.sh_c[q] = make_float4(c.x, c.y, c.z, 0.f);
+                P.sh_c[q] = make_float4(c.x, c.y, c.z, __int_as_float(rec));
             } else {  // no hit with t > 0 can be that close: always visible
                 float4 r = P.rad[slot];
                 P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+                if (NRC && rec >= 0) {
+                    float4 b = C.t_before[rec];
+                    C.t_before[rec] = make_float4(b.x + c.x, b.y + c.y, b.z + c.z, 0.f);
+                }
             }
         }
     }
+    if (NRC && query_here) return;
     if (pol.maxdepth > 0 && depth + 1 >= pol.maxdepth) return;
     // Russian roulette (rendererptls.cpp:80-83)
     float prr = depth < pol.rrdepth ? 1.0f : pol.prr;
@@ -311,9 +318,8 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     // contri = Li * |wi.n| * brdf / pdf / prr (rendererptls.cpp:90)
     f3 Tn = T * fabsf(dot(wi, normal)) * brdf / pdf / prr;
     f3 no = hit_pos + wi * 1e-3f;
-    const int oct = pol.sortdir ? ((wi.x < 0.f ? 1 : 0) | (wi.y < 0.f ? 2 : 0) | (wi.z < 0.f ? 4 : 0)) : 0;
-    int q = warp_append_keyed(oct, &P.counters[CNT_DIR_OUT]);
-    P.queue_out[(size_t)oct * capacity + q] = slot;
+    int q = warp_append(true, &P.counters[CNT_OUT]);
+    P.queue_out[q] = slot;
     P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
     P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
     P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
@@ -333,7 +339,7 @@ __global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Polic
 #pragma unroll
         for (int k = 1; k < NUM_CAT; ++k) if (i >= start[k]) c = k;
         int slot = P.sorted[(size_t)c * capacity + (i - start[c])];
-        shade_one<NRC>(P, S, pol, slot, C, capacity);
+        shade_one<NRC>(P, S, pol, slot, C);
     }
 }
 
@@ -346,13 +352,7 @@ __global__ void k_advance(uint32_t* counters) {
     unsigned long long* shr = reinterpret_cast<unsigned long long*>(counters + CNT_SHRAYS);
     *rays += in;
     *shr += sh;
-    uint32_t live = 0;
-    for (int k = 0; k < 8; ++k) {
-        live += counters[CNT_DIR_OUT + k];
-        counters[CNT_DIR_IN + k] = counters[CNT_DIR_OUT + k];
-        counters[CNT_DIR_OUT + k] = 0;
-    }
-    counters[CNT_IN] = live;
+    counters[CNT_IN] = counters[CNT_OUT];
     counters[CNT_OUT] = 0;
     counters[CNT_SHADOW] = 0;
     counters[CNT_WORK] = 0;
@@ -364,7 +364,7 @@ __global__ void k_advance(uint32_t* counters) {
 // CNT_RAYS on are kept for the whole render.
 __global__ void k_reset_counters(uint32_t* counters) {
     int i = threadIdx.x;
-    if ((i < CNT_RAYS && i != CNT_ERR) || (i >= CNT_DIR_IN && i < NUM_COUNTERS)) counters[i] = 0;
+    if (i < CNT_RAYS && i != CNT_ERR) counters[i] = 0;
 }
 
 // ---------------------------------------------------------------- film
@@ -420,29 +420,31 @@ __global__ void k_finish(const float4* film, int npix, float inv_spp, float* hdr
 
 // ---------------------------------------------------------------- online cache
 // Adds the cache prediction of each query: L += T * max(0, nrc(x)).
-__global__ void k_nrc_apply(PathState P, NrcCtx C, const float* __restrict__ pred, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int slot = C.q_slot[i];
-    float4 t = C.q_thr[i], r = P.rad[slot];
-    const float* o = pred + 3 * (size_t)i;
-    P.rad[slot] = make_float4(r.x + t.x * fmaxf(0.f, o[0]), r.y + t.y * fmaxf(0.f, o[1]), r.z + t.z * fmaxf(0.f, o[2]), 0.f);
+__global__ void k_nrc_apply(PathState P, NrcCtx C, const float* __restrict__ pred) {
+    const int n = (int)C.counters[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int slot = C.q_slot[i];
+        float4 t = C.q_thr[i], r = P.rad[slot];
+        const float* o = pred + 3 * (size_t)i;
+        P.rad[slot] = make_float4(r.x + t.x * fmaxf(0.f, o[0]), r.y + t.y * fmaxf(0.f, o[1]), r.z + t.z * fmaxf(0.f, o[2]), 0.f);
+    }
 }
 
 // Training targets: radiance the path gathered from the vertex on, divided by
 // the throughput that reached the vertex; channels with negligible
 // throughput copy the luminance-weighted value, and targets are clamped.
-__global__ void k_nrc_targets(PathState P, NrcCtx C, float* __restrict__ y, int n, float clamp_max) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int slot = C.t_slot[i];
-    float4 a = P.rad[slot], b = C.t_before[i], t = C.t_thr[i];
-    float d[3] = {a.x - b.x, a.y - b.y, a.z - b.z}, tt[3] = {t.x, t.y, t.z};
-    float tsum = tt[0] + tt[1] + tt[2], dsum = d[0] + d[1] + d[2];
-    for (int k = 0; k < 3; ++k) {
-        float v = tt[k] > 1e-4f ? d[k] / tt[k] : (tsum > 1e-4f ? dsum / tsum : 0.f);
-        if (!(v >= 0.f)) v = 0.f;  // NaN or negative
-        y[3 * (size_t)i + k] = fminf(v, clamp_max);
+__global__ void k_nrc_targets(PathState P, NrcCtx C, float* __restrict__ y, float clamp_max) {
+    const int n = min((int)C.counters[1], C.tcap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int slot = C.t_slot[i];
+        float4 a = P.rad[slot], b = C.t_before[i], t = C.t_thr[i];
+        float d[3] = {a.x - b.x, a.y - b.y, a.z - b.z}, tt[3] = {t.x, t.y, t.z};
+        float tsum = tt[0] + tt[1] + tt[2], dsum = d[0] + d[1] + d[2];
+        for (int k = 0; k < 3; ++k) {
+            float v = tt[k] > 1e-4f ? d[k] / tt[k] : (tsum > 1e-4f ? dsum / tsum : 0.f);
+            if (!(v >= 0.f)) v = 0.f;  // NaN or negative
+            y[3 * (size_t)i + k] = fminf(v, clamp_max);
+        }
     }
 }
 
@@ -479,9 +481,10 @@ __global__ void k_material_probe(DeviceScene S, int mat, int n, const float* wo,
 }
 
 // ---------------------------------------------------------------- launchers
-static int g_trace_blocks = 0, g_shadow_blocks = 0;
+static int g_trace_blocks = 0, g_shadow_blocks = 0, g_num_sms = 1;
 
 void launch_setup(int num_sms) {
+    g_num_sms = num_sms > 0 ? num_sms : 1;
     int b1 = 0, b2 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_trace<false, true>, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_shadow<false, true>, 128, 0);
@@ -509,23 +512,31 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
     if (nrc) k_shade<true><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, *nrc);
     else k_shade<false><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, NrcCtx{});
     if (ev) cudaEventRecord(ev[2], st);
+    float4* tb = (nrc && nrc->direct) ? nrc->t_before : nullptr;
     switch ((count ? 2 : 0) + pol.trav) {
-        case 0: k_shadow<false, false><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
-        case 1: k_shadow<false, true><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
-        case 2: k_shadow<true, false><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
-        default: k_shadow<true, true><<<g_shadow_blocks, 128, 0, st>>>(P, S); break;
+        case 0: k_shadow<false, false><<<g_shadow_blocks, 128, 0, st>>>(P, S, tb); break;
+        case 1: k_shadow<false, true><<<g_shadow_blocks, 128, 0, st>>>(P, S, tb); break;
+        case 2: k_shadow<true, false><<<g_shadow_blocks, 128, 0, st>>>(P, S, tb); break;
+        default: k_shadow<true, true><<<g_shadow_blocks, 128, 0, st>>>(P, S, tb); break;
     }
     if (ev) cudaEventRecord(ev[3], st);
     k_advance<<<1, 1, 0, st>>>(P.counters);
 }
 
-void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, NUM_COUNTERS, 0, st>>>(counters); }
+void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, 32, 0, st>>>(counters); }
 
-void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int n, cudaStream_t st) {
-    if (n > 0) k_nrc_apply<<<(n + 255) / 256, 256, 0, st>>>(P, C, pred, n);
+// The counts live on the device: grid-stride loops over a grid sized for
+// the capacity, at most eight 256-thread blocks per SM.
+static int count_grid(int cap) {
+    int b = (cap + 255) / 256;
+    const int most = 8 * g_num_sms;
+    return b < 1 ? 1 : (b > most ? most : b);
 }
-void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, int n, float clamp_max, cudaStream_t st) {
-    if (n > 0) k_nrc_targets<<<(n + 255) / 256, 256, 0, st>>>(P, C, y, n, clamp_max);
+void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int cap, cudaStream_t st) {
+    k_nrc_apply<<<count_grid(cap), 256, 0, st>>>(P, C, pred);
+}
+void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, float clamp_max, cudaStream_t st) {
+    k_nrc_targets<<<count_grid(C.tcap), 256, 0, st>>>(P, C, y, clamp_max);
 }
 
 void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, cudaStream_t st) {

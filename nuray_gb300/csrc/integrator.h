@@ -21,8 +21,9 @@ void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, 
 // trace + sort, shade, shadow, advance. ev (optional) receives 4 events.
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc);
-void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int n, cudaStream_t st);
-void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, int n, float clamp_max, cudaStream_t st);
+// Query and training-record counts are read from C.counters on the device.
+void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int cap, cudaStream_t st);
+void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, float clamp_max, cudaStream_t st);
 void launch_reset_counters(uint32_t* counters, cudaStream_t st);
 void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, cudaStream_t st);
 void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st);

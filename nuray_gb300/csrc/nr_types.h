@@ -65,7 +65,6 @@ struct Policy {
     uint32_t seed_lo, seed_hi;
     int32_t imgw, imgh;
     int32_t nee;      // 1: ptnee (RendererPTLS); 0: pt (RendererPT), no light sampling
-    int32_t sortdir;  // bucket continuing paths by direction octant (1) or keep one queue (0)
     int32_t trav;     // traversal tests: 0 exact arithmetic only, 1 fast path with exact fallback (same hits)
 };
 
@@ -77,9 +76,7 @@ struct PathState {
     float4* thr;     // (throughput, light_fac)
     float4* rad;     // (radiance, unused)
     uint4* meta;     // (pixel, sample, draws taken, vertex depth)
-    // queues of slot indices, eight segments of `capacity` entries each: the
-    // continuing paths are bucketed by the octant of their direction so a
-    // warp of the next traversal mostly holds rays of one octant
+    // queues of slot indices
     int32_t* queue_in;
     int32_t* queue_out;
     int32_t* sorted;      // slots bucketed by shading category
@@ -107,6 +104,9 @@ struct NrcCtx {
     int32_t query;          // 0: train only (every path runs to the end)
     int32_t min_depth;      // first vertex depth at which the cache may end a path
     float rough;            // GGX roughness from which a vertex counts as diffuse
+    int32_t train_depth;    // > 0: training paths end in the cache from this vertex depth on
+    int32_t direct;         // 1: the cache holds radiance after the vertex's own light sample
+                            // (queries still sample a light); 0: all outgoing radiance
     float lo[3], inv_ext[3];  // scene box for the position encoding
 };
 
@@ -133,9 +133,7 @@ enum Counter {
     CNT_TRIS = 24,     // triangles tested by closest-hit rays,
     CNT_SH_NODES = 26, // nodes visited by shadow rays,
     CNT_SH_TRIS = 28,  // triangles tested by shadow rays
-    CNT_DIR_IN = 32,   // 32..39: queue_in entries per direction octant
-    CNT_DIR_OUT = 40,  // 40..47: queue_out entries per direction octant
-    NUM_COUNTERS = 48
+    NUM_COUNTERS = 32
 };
 
 }  // namespace nr

@@ -41,6 +41,15 @@ __device__ __forceinline__ uint32_t pack2h(__nv_bfloat16 lo, __nv_bfloat16 hi) {
 }
 __device__ __forceinline__ float bf(const __nv_bfloat16 x) { return __bfloat162float(x); }
 
+// First row and row count of a launch (see NrcRows).
+__device__ __forceinline__ void row_range(const NrcRows& R, int& m0, int& M) {
+    if (!R.count) { m0 = 0; M = R.n; return; }
+    const int total = min((int)*R.count, R.n);
+    const int chunk = (total + R.steps - 1) / R.steps;
+    m0 = R.step * chunk;
+    M = max(0, min(chunk, total - m0));
+}
+
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -123,8 +132,14 @@ __device__ __forceinline__ void relu_to_a(float (&acc)[8][4], uint32_t (&a)[4][4
 // null): [4][M][64] BF16 post-ReLU activations of the hidden layers, kept for
 // the backward pass.
 __global__ void __launch_bounds__(128) k_nrc_forward(const __nv_bfloat16* __restrict__ wb, const float* __restrict__ params,
-                                                     const __nv_bfloat16* __restrict__ x, int M, float* __restrict__ out,
+                                                     const __nv_bfloat16* __restrict__ x, NrcRows R, float* __restrict__ out,
                                                      __nv_bfloat16* __restrict__ acts) {
+    int m0, M;
+    row_range(R, m0, M);
+    if (M <= 0 || (int)blockIdx.x * 64 >= M) return;
+    x += (size_t)m0 * IN;
+    out += (size_t)m0 * 3;
+    const size_t LS = (size_t)R.ld * H;  // one layer of acts
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
     float* sb = reinterpret_cast<float*>(sw + SM_WEND);
@@ -152,13 +167,13 @@ __global__ void __launch_bounds__(128) k_nrc_forward(const __nv_bfloat16* __rest
         float acc[8][4];
         uint32_t a[4][4];
         layer_fwd<5>(acc, a0, sw + SM_W0, S0, sb, g, t);
-        relu_to_a(acc, a, acts ? acts + 0 * (size_t)M * H : nullptr, row0, M, g, t);
+        relu_to_a(acc, a, acts ? acts + 0 * LS : nullptr, row0, M, g, t);
         layer_fwd<4>(acc, a, sw + SM_W1, SH, sb + H, g, t);
-        relu_to_a(acc, a, acts ? acts + 1 * (size_t)M * H : nullptr, row0, M, g, t);
+        relu_to_a(acc, a, acts ? acts + 1 * LS : nullptr, row0, M, g, t);
         layer_fwd<4>(acc, a, sw + SM_W2, SH, sb + 2 * H, g, t);
-        relu_to_a(acc, a, acts ? acts + 2 * (size_t)M * H : nullptr, row0, M, g, t);
+        relu_to_a(acc, a, acts ? acts + 2 * LS : nullptr, row0, M, g, t);
         layer_fwd<4>(acc, a, sw + SM_W3, SH, sb + 3 * H, g, t);
-        relu_to_a(acc, a, acts ? acts + 3 * (size_t)M * H : nullptr, row0, M, g, t);
+        relu_to_a(acc, a, acts ? acts + 3 * LS : nullptr, row0, M, g, t);
         // output layer, one n-tile of 8 (3 used)
         float o[4] = {sb[4 * H + 2 * t], sb[4 * H + 2 * t + 1], sb[4 * H + 2 * t], sb[4 * H + 2 * t + 1]};
 #pragma unroll
@@ -180,12 +195,19 @@ __global__ void __launch_bounds__(128) k_nrc_forward(const __nv_bfloat16* __rest
 
 // Backward through the layers for M rows: loss gradient of the relative L2
 // loss (o - y)^2 / (o^2 + 0.01) (o held constant in the denominator), then
-// dZ_l for every layer, stored as BF16 [5][M][64] (layer 4 uses 8 columns).
-// loss_sum (FP32, may be null) receives the summed loss.
+// dZ_l for every layer, stored as BF16 [5][ld][64] (layer 4 uses 8 columns).
+// loss_sum (FP32, may be null) receives the mean loss over the rows.
 __global__ void __launch_bounds__(128) k_nrc_backward_data(const __nv_bfloat16* __restrict__ wb,
                                                            const float* __restrict__ out, const float* __restrict__ y,
-                                                           const __nv_bfloat16* __restrict__ acts, int M, float inv_n,
+                                                           const __nv_bfloat16* __restrict__ acts, NrcRows R,
                                                            __nv_bfloat16* __restrict__ dz, float* loss_sum) {
+    int m0, M;
+    row_range(R, m0, M);
+    if (M <= 0 || (int)blockIdx.x * 64 >= M) return;
+    out += (size_t)m0 * 3;
+    y += (size_t)m0 * 3;
+    const float inv_n = 1.0f / (3.0f * (float)M);
+    const size_t LS = (size_t)R.ld * H;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
     load_weights(wb, sw);
@@ -213,7 +235,7 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data(const __nv_bfloat16* 
                 }
                 d4[2 * h + e] = v;
             }
-        __nv_bfloat16* dz4 = dz + 4 * (size_t)M * H;
+        __nv_bfloat16* dz4 = dz + 4 * LS;
         for (int h = 0; h < 2; ++h)
             if (rr[h] < M) *reinterpret_cast<uint32_t*>(dz4 + (size_t)rr[h] * H + 2 * t) = pack2(d4[2 * h], d4[2 * h + 1]);
         // dA3 = dOut x W4 (contraction over the 16 padded outputs)
@@ -235,8 +257,8 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data(const __nv_bfloat16* 
         // hidden layers 3, 2, 1, 0: dZ_l = dA_l * (A_l > 0); dA_{l-1} = dZ_l x W_l
 #pragma unroll 1
         for (int l = 3; l >= 0; --l) {
-            const __nv_bfloat16* act = acts + (size_t)l * M * H;
-            __nv_bfloat16* dzl = dz + (size_t)l * M * H;
+            const __nv_bfloat16* act = acts + (size_t)l * LS;
+            __nv_bfloat16* dzl = dz + (size_t)l * LS;
 #pragma unroll
             for (int jt = 0; jt < 8; ++jt)
 #pragma unroll
@@ -275,17 +297,30 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data(const __nv_bfloat16* 
     if (loss_sum) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-        if (lane == 0) atomicAdd(loss_sum, loss);
+        if (lane == 0) atomicAdd(loss_sum, loss * (1.0f / (3.0f * (float)M)));
     }
 }
 
-// Weight gradient of one layer: gW[n][k] += sum_m dZ[m][n] X[m][k] and
-// gb[n] += sum_m dZ[m][n] over M rows, split over CTAs in 64-row chunks.
-// N is 64 (hidden) or 8 (output); K is 80 (input layer) or 64. X rows have
-// stride K, dZ rows stride 64.
-__global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16* __restrict__ dz,
-                                                             const __nv_bfloat16* __restrict__ xin, int M, int N, int K,
-                                                             float* __restrict__ gW, float* __restrict__ gb) {
+// Weight gradients of all five layers in one launch (blockIdx.y = layer):
+// gW[n][k] += sum_m dZ[m][n] X[m][k] and gb[n] += sum_m dZ[m][n], split
+// over CTAs in 64-row chunks. N is 64 (hidden) or 8 (output); K is 80 (input
+// layer) or 64. X rows have stride K, dZ rows stride 64.
+__global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16* __restrict__ dz_all,
+                                                             const __nv_bfloat16* __restrict__ x,
+                                                             const __nv_bfloat16* __restrict__ acts, NrcRows R,
+                                                             float* __restrict__ grad) {
+    int row0, M;
+    row_range(R, row0, M);
+    if (M <= 0 || (int)blockIdx.x * 64 >= M) return;
+    const int l = blockIdx.y;
+    const size_t LS = (size_t)R.ld * H;
+    const int N = l == 4 ? OP : H, K = l == 0 ? IN : H;
+    const __nv_bfloat16* dz = dz_all + (size_t)l * LS;
+    const __nv_bfloat16* xin = l == 0 ? x + (size_t)row0 * IN : acts + (size_t)(l - 1) * LS;
+    const int woff = l == 0 ? NRC_OFF_W0 : (l == 1 ? NRC_OFF_W1 : (l == 2 ? NRC_OFF_W2 : (l == 3 ? NRC_OFF_W3 : NRC_OFF_W4)));
+    const int boff = l == 0 ? NRC_OFF_B0 : (l == 1 ? NRC_OFF_B1 : (l == 2 ? NRC_OFF_B2 : (l == 3 ? NRC_OFF_B3 : NRC_OFF_B4)));
+    float* gW = grad + woff;
+    float* gb = grad + boff;
     __shared__ __align__(16) __nv_bfloat16 sdz[64 * (H + 8)];
     __shared__ __align__(16) __nv_bfloat16 sx[64 * (IN + 8)];
     const int SD = H + 8, SX = K + 8;
@@ -354,9 +389,12 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
 __global__ void k_nrc_adam(float* __restrict__ p, float* __restrict__ grad, float* __restrict__ m, float* __restrict__ v,
                            __nv_bfloat16* __restrict__ wb, float* __restrict__ ema, float* __restrict__ pinf,
                            __nv_bfloat16* __restrict__ wb_inf, int n, float lr, float b1, float b2, float eps, float c1,
-                           float c2, float beta, float cema) {
+                           float c2, float beta, float cema, NrcRows R) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    int r0, rows;
+    row_range(R, r0, rows);
+    if (rows <= 0) return;  // an empty counted chunk: no step
     float gr = grad[i];
     float mi = b1 * m[i] + (1.f - b1) * gr;
     float vi = b2 * v[i] + (1.f - b2) * gr * gr;
@@ -393,40 +431,41 @@ static int grid_for(int tiles, int num_sms) {
     return blocks < 1 ? 1 : (blocks > cap ? cap : blocks);
 }
 
-void nrc_launch_forward(const NrcDev& N, const __nv_bfloat16* x, int M, float* out, __nv_bfloat16* acts, int num_sms,
-                        cudaStream_t st) {
+// Largest number of rows a launch over R can see.
+static int max_rows(const NrcRows& R) { return R.count ? (R.n + R.steps - 1) / R.steps : R.n; }
+
+void nrc_launch_forward(const NrcDev& N, const __nv_bfloat16* x, const NrcRows& R, float* out, __nv_bfloat16* acts,
+                        int num_sms, cudaStream_t st) {
+    const int M = max_rows(R);
     if (M <= 0) return;
-    k_nrc_forward<<<grid_for((M + 15) / 16, num_sms), 128, nrc_forward_smem(), st>>>(N.wb, N.params, x, M, out, acts);
+    k_nrc_forward<<<grid_for((M + 15) / 16, num_sms), 128, nrc_forward_smem(), st>>>(N.wb, N.params, x, R, out, acts);
 }
 
 void nrc_launch_backward(const NrcDev& N, const __nv_bfloat16* x, const float* out, const float* y,
-                         const __nv_bfloat16* acts, __nv_bfloat16* dz, int M, float* loss_sum, int num_sms,
+                         const __nv_bfloat16* acts, __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms,
                          cudaStream_t st) {
+    const int M = max_rows(R);
     if (M <= 0) return;
-    k_nrc_backward_data<<<grid_for((M + 15) / 16, num_sms), 128, nrc_backward_smem(), st>>>(
-        N.wb, out, y, acts, M, 1.0f / (3.0f * (float)M), dz, loss_sum);
+    k_nrc_backward_data<<<grid_for((M + 15) / 16, num_sms), 128, nrc_backward_smem(), st>>>(N.wb, out, y, acts, R, dz,
+                                                                                          loss_sum);
     int blocks = (M + 63) / 64;
     if (blocks > num_sms * 2) blocks = num_sms * 2;
-    const size_t MH = (size_t)M * H;
-    const int woff[5] = {NRC_OFF_W0, NRC_OFF_W1, NRC_OFF_W2, NRC_OFF_W3, NRC_OFF_W4};
-    const int boff[5] = {NRC_OFF_B0, NRC_OFF_B1, NRC_OFF_B2, NRC_OFF_B3, NRC_OFF_B4};
-    for (int l = 0; l < 5; ++l) {
-        const __nv_bfloat16* xin = l == 0 ? x : acts + (size_t)(l - 1) * MH;
-        k_nrc_backward_weight<<<blocks, 128, 0, st>>>(dz + (size_t)l * MH, xin, M, l == 4 ? OP : H, l == 0 ? IN : H,
-                                                      N.grad + woff[l], N.grad + boff[l]);
-    }
+    k_nrc_backward_weight<<<dim3(blocks, 5), 128, 0, st>>>(dz, x, acts, R, N.grad);
 }
 
-void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta, cudaStream_t st) {
+void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta,
+                     const NrcRows& R, cudaStream_t st) {
     float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
     float cema = 1.f - powf(ema_beta, (float)step);
     k_nrc_adam<<<(NRC_NUM_PARAMS + 255) / 256, 256, 0, st>>>(N.params, N.grad, N.m, N.v, N.wb, N.ema, N.pinf, N.wb_inf,
-                                                            NRC_NUM_PARAMS, lr, b1, b2, eps, c1, c2, ema_beta, cema);
+                                                            NRC_NUM_PARAMS, lr, b1, b2, eps, c1, c2, ema_beta, cema, R);
 }
 
-void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, int M, float* out, int num_sms, cudaStream_t st) {
+void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, const NrcRows& R, float* out, int num_sms,
+                            cudaStream_t st) {
+    const int M = max_rows(R);
     if (M <= 0) return;
-    k_nrc_forward<<<grid_for((M + 15) / 16, num_sms), 128, nrc_forward_smem(), st>>>(N.wb_inf, N.pinf, x, M, out, nullptr);
+    k_nrc_forward<<<grid_for((M + 15) / 16, num_sms), 128, nrc_forward_smem(), st>>>(N.wb_inf, N.pinf, x, R, out, nullptr);
 }
 
 void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t st) {

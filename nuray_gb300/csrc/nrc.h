@@ -38,19 +38,40 @@ struct NrcDev {
     __nv_bfloat16* wb_inf;
 };
 
+// The rows one launch works on. With count == nullptr they are [0, n). With
+// a device counter they are chunk `step` of `steps` equal chunks of
+// min(*count, n) rows, so a whole training sequence can be issued before
+// the host knows how many rows there are. Per-row arrays (x, y, out) are
+// indexed from the first row of the chunk; acts and dz hold one chunk with
+// `ld` rows per layer.
+struct NrcRows {
+    const uint32_t* count;
+    int n;
+    int step, steps;
+    int ld;
+};
+inline NrcRows nrc_rows(int n) { return NrcRows{nullptr, n, 0, 1, n}; }
+inline NrcRows nrc_rows_counted(const uint32_t* count, int n, int step, int steps) {
+    return NrcRows{count, n, step, steps, (n + steps - 1) / steps};
+}
+
 void nrc_setup();
-// out [M][3] FP32; acts [4][M][64] BF16 or null.
-void nrc_launch_forward(const NrcDev& N, const __nv_bfloat16* x, int M, float* out, __nv_bfloat16* acts, int num_sms,
-                        cudaStream_t st);
-// Accumulates the gradient of the mean relative L2 loss into N.grad;
-// dz: [5][M][64] BF16 scratch; loss_sum (device float, may be null) gets the summed loss.
+// out [rows][3] FP32; acts [4][ld][64] BF16 or null.
+void nrc_launch_forward(const NrcDev& N, const __nv_bfloat16* x, const NrcRows& R, float* out, __nv_bfloat16* acts,
+                        int num_sms, cudaStream_t st);
+// Accumulates the gradient of the mean relative L2 loss of the chunk into
+// N.grad; dz: [5][ld][64] BF16 scratch; loss_sum (device float, may be null)
+// gets the chunk's mean loss added.
 void nrc_launch_backward(const NrcDev& N, const __nv_bfloat16* x, const float* out, const float* y,
-                         const __nv_bfloat16* acts, __nv_bfloat16* dz, int M, float* loss_sum, int num_sms,
+                         const __nv_bfloat16* acts, __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms,
                          cudaStream_t st);
-// ema_beta 0 keeps pinf / wb_inf equal to the current parameters.
-void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta, cudaStream_t st);
+// ema_beta 0 keeps pinf / wb_inf equal to the current parameters. A counted
+// chunk without rows leaves the parameters unchanged.
+void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta,
+                     const NrcRows& R, cudaStream_t st);
 // Forward with the inference copy (pinf / wb_inf).
-void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, int M, float* out, int num_sms, cudaStream_t st);
+void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, const NrcRows& R, float* out, int num_sms,
+                            cudaStream_t st);
 void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t st);
 
 }  // namespace nr

@@ -125,6 +125,35 @@ def test_port_equals_reference_mixed(port_lib, ref_lib, seed):
         np.testing.assert_array_equal(a, b)
 
 
+def test_port_equals_reference_procedural_terrain(port_lib, ref_lib):
+    """A reduced version of the 1M-triangle procedural scene (fBm terrain with
+    shared vertices, spheres, 16 quad lights, GGX-reflect materials of every
+    roughness) under the reference's own policy (RR from vertex 0, prr 0.8,
+    no depth limit; the reference has no rrdepth / maxdepth keys): the same
+    tree, the same hits from surface points, the same radiance per sample."""
+    sc = scenes.terrain_spheres(4, tiles=12, cells_per_tile=8, spheres=24, slices=16, stacks=12, lights=16,
+                                n_mats=24, extent=96.0)
+    P, R = Oracle("port", sc), Oracle("ref", sc)
+    for a, b in zip(P.bvh(), R.bvh()):
+        np.testing.assert_array_equal(a, b)
+    params = ("renderer=ptnee imgw=320 imgh=180 campos=0,40,60 cameuler=0,-40,0 camfov=45 camasp=1.7778")
+    pix = pixel_grid(320, 180)[::7]
+    a, b = P.render_samples(params, pix, 4, seed=9), R.render_samples(params, pix, 4, seed=9)
+    assert (a.sum(2) > 0).mean() > 0.3  # the sample sees lit geometry
+    np.testing.assert_array_equal(a, b)
+    # rays leaving surface points, as shadow and continuation rays do
+    rng = np.random.default_rng(4)
+    pos = sc["pos"].reshape(-1, 3, 3)
+    ti = rng.integers(0, pos.shape[0], 20000)
+    w = rng.dirichlet((1, 1, 1), 20000)
+    p = np.einsum("nk,nkc->nc", w, pos[ti]).astype(np.float32)
+    d = rng.normal(size=(20000, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    o = (p + d * np.float32(1e-3)).astype(np.float32)
+    for x, y in zip(P.intersect(o, d), R.intersect(o, d)):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_port_equals_reference_plain_pt(port_lib, ref_lib):
     """renderer=pt: RendererPT::trace (src/renderer/rendererpt.cpp:13-59)."""
     sc = scenes.small_scene(6)
