@@ -415,7 +415,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.tile = c.get_int("tile", 1) != 0;
     a.nrc = c.get_int("nrc", 0) != 0;
     a.nrc_train = c.get_int("nrc_train", 16384);
-    a.nrc_steps = c.get_int("nrc_steps", 4);
+    a.nrc_steps = c.get_int("nrc_steps", 2);
     a.nrc_query = c.get_int("nrc_query", 1);
     a.nrc_mindepth = c.get_int("nrc_mindepth", 1);
     a.nrc_rough = c.get_float("nrc_rough", 0.2f);

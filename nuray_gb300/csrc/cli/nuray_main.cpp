@@ -9,8 +9,9 @@
 // renderer must be ptnee or pt (the reference also selects bdpt, pm, pssmlt
 // and nrc; those are not implemented here and are rejected). envmap= (PFM or binary
 // PPM) and envmap_gain= attach an environment map as the reference CLI does.
-// The output is written as BMP (24-bit, what QImage::save produces for an
-// RGB888 image), PPM (8-bit) or PFM (the linear HDR mean), by extension.
+// The output is written by extension as PNG (8-bit RGB), BMP (24-bit, what
+// QImage::save produces for an RGB888 image), PPM (8-bit) or PFM (the linear
+// HDR mean); other extensions get BMP.
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -22,6 +23,7 @@
 
 #include "../../../include/nuray_renderer.hpp"
 #include "../host_scene.h"
+#include "../image_io.h"
 
 namespace {
 
@@ -37,7 +39,10 @@ bool write_image(const std::string& path, const nr::Image& img) {
     std::ofstream f(path, std::ios::binary);
     if (!f) return false;
     const int w = img.width, h = img.height;
-    if (ends_with(path, ".pfm")) {
+    if (ends_with(path, ".png")) {
+        std::vector<uint8_t> png = nr::png_encode_rgb8(img.rgb.data(), w, h);
+        f.write(reinterpret_cast<const char*>(png.data()), (std::streamsize)png.size());
+    } else if (ends_with(path, ".pfm")) {
         f << "PF\n" << w << " " << h << "\n-1.0\n";
         for (int y = h - 1; y >= 0; --y) f.write(reinterpret_cast<const char*>(&img.hdr[(size_t)y * w * 3]), (size_t)w * 12);
     } else if (ends_with(path, ".ppm")) {

@@ -1,6 +1,7 @@
 // Host side of libnuray_gpu.so: parameter grammar, scene loading and
 // flattening, reference SAH BVH build. See host_scene.h.
 #include "host_scene.h"
+#include "image_io.h"
 
 #include <algorithm>
 #include <atomic>
@@ -143,6 +144,29 @@ std::string scene_from_desc(const nr_scene_desc& d, HostScene& s) {
 std::string read_image(const std::string& path, int& w, int& h, std::vector<float>& rgb) {
     std::ifstream f(path, std::ios::binary);
     if (!f) return "cannot open " + path;
+    {
+        unsigned char sig[8] = {0};
+        f.read(reinterpret_cast<char*>(sig), 8);
+        if (f.gcount() == 8 && sig[0] == 0x89 && sig[1] == 'P' && sig[2] == 'N' && sig[3] == 'G') {
+            f.seekg(0, std::ios::end);
+            std::vector<uint8_t> bytes((size_t)f.tellg());
+            f.seekg(0);
+            f.read(reinterpret_cast<char*>(bytes.data()), (std::streamsize)bytes.size());
+            if (!f) return "cannot read " + path;
+            std::vector<uint8_t> rgba;
+            std::string err = png_decode(bytes, w, h, rgba);
+            if (!err.empty()) return err + ": " + path;
+            // Texture::load: QColor::redF() = (8-bit value * 257) / 65535 as a
+            // double, then pow(., 2.2f) (src/scene/texture.cpp:13-19)
+            rgb.resize((size_t)w * h * 3);
+            for (size_t i = 0; i < (size_t)w * h; ++i)
+                for (int k = 0; k < 3; ++k)
+                    rgb[3 * i + k] = (float)std::pow((double)(rgba[4 * i + k] * 257) / 65535.0, (double)2.2f);
+            return "";
+        }
+        f.clear();
+        f.seekg(0);
+    }
     std::string magic;
     f >> magic;
     if (magic == "PF" || magic == "Pf") {
@@ -183,7 +207,7 @@ std::string read_image(const std::string& path, int& w, int& h, std::vector<floa
         for (size_t i = 0; i < raw.size(); ++i) rgb[i] = (float)std::pow(raw[i] / 255.0, (double)2.2f);
         return "";
     }
-    return "unsupported image format (PFM or binary PPM): " + path;
+    return "unsupported image format (PNG, PFM or binary PPM): " + path;
 }
 
 // ------------------------------------------------------------------ OBJ / MTL

@@ -52,13 +52,14 @@ struct HostScene {
 std::string scene_from_desc(const nr_scene_desc& d, HostScene& out);
 
 // Loader::fromSceneDescription / loadObj / loadMtl (src/scene/loader.cpp).
-// Texture maps referenced by MTL files must be PFM or binary PPM files
-// (the reference decodes PNG/JPG through Qt, which this library does not
-// link). Returns "" or an error message.
+// Texture maps referenced by MTL files may be PNG, PFM or binary PPM files
+// (the reference decodes through Qt, which also reads JPG; JPG is not
+// supported here). Returns "" or an error message.
 std::string scene_from_text(const std::string& desc, HostScene& out);
 
-// Reads a PFM (float) or binary PPM (8-bit, decoded with c^2.2 as
-// Texture::load does) image into linear RGB floats.
+// Reads a PNG or binary PPM (8-bit, decoded with c^2.2 as Texture::load
+// does) or a PFM (float, used as is) image into linear RGB floats, row 0 at
+// the top.
 std::string read_image(const std::string& path, int& w, int& h, std::vector<float>& rgb);
 
 // Binary BVH with the reference's SAH (BVH::_divide, src/hierarchy/bvh.cpp:5-58):

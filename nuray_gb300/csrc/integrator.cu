@@ -101,8 +101,17 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // return the same hits bit for bit. (Measured and dropped: a variant that
 // refilled idle lanes from the queue with separate node and leaf phases,
 // 28 % slower; a four-wide tree collapsed from this one, no faster.)
+// Minimum resident 128-thread blocks per SM requested from the register
+// allocator for the two traversal kernels (occupancy against registers).
+#ifndef NR_TRACE_MINB
+#define NR_TRACE_MINB 1
+#endif
+#ifndef NR_SHADOW_MINB
+#define NR_SHADOW_MINB 1
+#endif
+
 template <bool COUNT, bool FAST>
-__global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int capacity) {
+__global__ void __launch_bounds__(128, NR_TRACE_MINB) k_trace(PathState P, DeviceScene S, int capacity) {
     const uint32_t n = P.counters[CNT_IN];
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
@@ -134,7 +143,7 @@ __global__ void __launch_bounds__(128) k_trace(PathState P, DeviceScene S, int c
 // Shadow rays, persistent like k_trace: occluded when any reachable triangle
 // has t <= the ray's limit (any_hit); unoccluded rays add their NEE term.
 template <bool COUNT, bool FAST>
-__global__ void __launch_bounds__(128) k_shadow(PathState P, DeviceScene S, float4* t_before) {
+__global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, DeviceScene S, float4* t_before) {
     const uint32_t n = P.counters[CNT_SHADOW];
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;

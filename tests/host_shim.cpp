@@ -5,6 +5,7 @@
 #include <string>
 
 #include "host_scene.h"
+#include "image_io.h"
 
 extern "C" {
 
@@ -56,5 +57,39 @@ int shim_config_vec3(const char* params, const char* key, float* out) { return n
 void shim_camera(const char* params, nr_camera* cam, float* film_h) {
     *cam = nr::camera_from_config(nr::Config(params));
     *film_h = nr::film_height(*cam);
+}
+
+// PNG bytes -> RGBA8. Returns 0, or -1 with the message in err. rgba may be
+// null to read the size only.
+int shim_png_decode(const unsigned char* bytes, long n, int* w, int* h, unsigned char* rgba, char* err, int errlen) {
+    std::vector<uint8_t> f(bytes, bytes + n), out;
+    std::string e = nr::png_decode(f, *w, *h, out);
+    if (!e.empty()) {
+        std::strncpy(err, e.c_str(), (size_t)errlen - 1);
+        err[errlen - 1] = 0;
+        return -1;
+    }
+    if (rgba) std::memcpy(rgba, out.data(), out.size());
+    return 0;
+}
+
+// RGB8 -> PNG bytes; returns the size (out may be null to size it).
+long shim_png_encode(const unsigned char* rgb, int w, int h, unsigned char* out) {
+    std::vector<uint8_t> png = nr::png_encode_rgb8(rgb, w, h);
+    if (out) std::memcpy(out, png.data(), png.size());
+    return (long)png.size();
+}
+
+// Texture file -> linear RGB floats as the scene loader reads it.
+int shim_read_image(const char* path, int* w, int* h, float* rgb, char* err, int errlen) {
+    std::vector<float> v;
+    std::string e = nr::read_image(path, *w, *h, v);
+    if (!e.empty()) {
+        std::strncpy(err, e.c_str(), (size_t)errlen - 1);
+        err[errlen - 1] = 0;
+        return -1;
+    }
+    if (rgb) std::memcpy(rgb, v.data(), v.size() * sizeof(float));
+    return 0;
 }
 }

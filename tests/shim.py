@@ -12,8 +12,10 @@ CSRC = os.path.join(ROOT, "nuray_gb300", "csrc")
 
 
 def load():
-    srcs = [os.path.join(ROOT, "tests", "host_shim.cpp"), os.path.join(CSRC, "host_scene.cpp")]
-    deps = srcs + [os.path.join(CSRC, "host_scene.h"), os.path.join(ROOT, "include", "nuray.h")]
+    srcs = [os.path.join(ROOT, "tests", "host_shim.cpp"), os.path.join(CSRC, "host_scene.cpp"),
+            os.path.join(CSRC, "image_io.cpp")]
+    deps = srcs + [os.path.join(CSRC, "host_scene.h"), os.path.join(CSRC, "image_io.h"),
+                   os.path.join(ROOT, "include", "nuray.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(p) > os.path.getmtime(LIB) for p in deps):
         os.makedirs(OUT, exist_ok=True)
         subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", CSRC, "-I",
@@ -27,7 +29,41 @@ def load():
     L.shim_config_float.restype = ctypes.c_float
     L.shim_config_vec3.argtypes = [ctypes.c_char_p, ctypes.c_char_p, vp]
     L.shim_camera.argtypes = [ctypes.c_char_p, vp, vp]
+    L.shim_png_decode.argtypes = [ctypes.c_char_p, ctypes.c_long, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
+    L.shim_png_encode.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+    L.shim_png_encode.restype = ctypes.c_long
+    L.shim_read_image.argtypes = [ctypes.c_char_p, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
     return L
+
+
+def png_decode(L, data):
+    """PNG bytes -> (h, w, 4) uint8 through the product decoder; raises ValueError."""
+    w, h = ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    if L.shim_png_decode(data, len(data), ctypes.byref(w), ctypes.byref(h), None, err, 256) != 0:
+        raise ValueError(err.value.decode())
+    out = np.zeros((h.value, w.value, 4), np.uint8)
+    L.shim_png_decode(data, len(data), ctypes.byref(w), ctypes.byref(h), out.ctypes.data, err, 256)
+    return out
+
+
+def png_encode(L, rgb):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    h, w = rgb.shape[:2]
+    n = L.shim_png_encode(rgb.ctypes.data, w, h, None)
+    out = np.zeros(n, np.uint8)
+    L.shim_png_encode(rgb.ctypes.data, w, h, out.ctypes.data)
+    return out.tobytes()
+
+
+def read_image(L, path):
+    w, h = ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    if L.shim_read_image(path.encode(), ctypes.byref(w), ctypes.byref(h), None, err, 256) != 0:
+        raise ValueError(err.value.decode())
+    out = np.zeros((h.value, w.value, 3), np.float32)
+    L.shim_read_image(path.encode(), ctypes.byref(w), ctypes.byref(h), out.ctypes.data, err, 256)
+    return out
 
 
 def bvh(L, pos, threads=4):
