@@ -163,6 +163,20 @@ int nr_scene_set_env(nr_scene* scene, int32_t width, int32_t height, const float
 /* info[0..5] = triangles, materials, BVH nodes, BVH depth, emitters, device bytes. */
 int nr_scene_info(const nr_scene* scene, int64_t info[6]);
 
+/* nr_scene_create / nr_scene_load with options ("key=value ..."; NULL or
+ * "" for the defaults). bvh=host (default) builds the reference's SAH tree
+ * (BVH::_build, src/hierarchy/bvh.cpp:60-70) on the host threads; bvh=gpu
+ * builds it on the device, level by level: the same cost and split rule,
+ * the same tree wherever no two triangles share a pMax coordinate, and a
+ * stable (loader-index) order among equal keys where the reference's
+ * std::sort order is unspecified. No reference counterpart for the option. */
+int nr_scene_create_opts(const nr_scene_desc* desc, const char* options, nr_scene** out);
+int nr_scene_load_opts(const char* text, const char* options, nr_scene** out);
+
+/* Wall-clock time of the scene's BVH build and, for bvh=gpu, the device
+ * time of its kernels (0 for the host build). No reference counterpart. */
+int nr_scene_build_times(const nr_scene* scene, double* bvh_wall_ms, double* bvh_device_ms);
+
 /* Reads back the flattened scene in loader order (pos 9, uv 6, nrm 9 floats
  * and a material index per triangle; materials) for checks. Any pointer may
  * be NULL. */

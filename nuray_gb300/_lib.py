@@ -58,6 +58,9 @@ SIGNATURES = {
     "nr_last_error": [_cp, ctypes.c_size_t],
     "nr_scene_create": [_vp, _vp],
     "nr_scene_load": [_cp, _vp],
+    "nr_scene_create_opts": [_vp, _cp, _vp],
+    "nr_scene_load_opts": [_cp, _cp, _vp],
+    "nr_scene_build_times": [_vp, _vp, _vp],
     "nr_scene_destroy": [_vp],
     "nr_scene_set_env": [_vp, _i32, _i32, _vp, ctypes.c_float],
     "nr_scene_info": [_vp, _vp],
@@ -122,13 +125,13 @@ class Scene:
         self._h = ctypes.c_void_p(handle)
 
     @classmethod
-    def from_text(cls, desc):
+    def from_text(cls, desc, options=""):
         h = ctypes.c_void_p()
-        check(lib().nr_scene_load(desc.encode(), ctypes.byref(h)))
+        check(lib().nr_scene_load_opts(desc.encode(), options.encode(), ctypes.byref(h)))
         return cls(h.value)
 
     @classmethod
-    def from_arrays(cls, pos, mat, mats, uv=None, nrm=None, textures=(), env_tex=-1, env_gain=1.0):
+    def from_arrays(cls, pos, mat, mats, uv=None, nrm=None, textures=(), env_tex=-1, env_gain=1.0, options=""):
         """pos (n,9) float32, mat (n,) int32, mats: list of dicts / Material,
         textures: list of (h, w, 3) float32 arrays (row 0 at v = 1)."""
         pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 9)
@@ -145,8 +148,14 @@ class Scene:
         d = SceneDesc(n, _ptr(pos), _ptr(uv), _ptr(nrm), _ptr(mat), len(mats), ctypes.addressof(mt), len(textures),
                       _ptr(wh) if len(textures) else None, _ptr(td) if len(textures) else None, env_tex, env_gain)
         h = ctypes.c_void_p()
-        check(lib().nr_scene_create(ctypes.byref(d), ctypes.byref(h)))
+        check(lib().nr_scene_create_opts(ctypes.byref(d), options.encode(), ctypes.byref(h)))
         return cls(h.value)
+
+    def build_times(self):
+        """(wall ms, device ms) of the scene's BVH build."""
+        w, d = ctypes.c_double(), ctypes.c_double()
+        check(lib().nr_scene_build_times(self._h, ctypes.byref(w), ctypes.byref(d)))
+        return w.value, d.value
 
     def close(self):
         if self._h:

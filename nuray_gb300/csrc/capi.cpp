@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/nuray.h"
+#include "bvh_gpu.h"
 #include "host_scene.h"
 #include "integrator.h"
 #include "nrc.h"
@@ -132,6 +133,7 @@ struct nr_scene {
     nr::NrcCtx nrc_ctx{};
     float* nrc_pred = nullptr;
     float nrc_last_loss = 0.f;
+    double bvh_wall_ms = 0.0, bvh_device_ms = 0.0;  // last BVH build
 
     ~nr_scene() {
         if (device >= 0) cudaSetDevice(device);
@@ -291,13 +293,24 @@ void upload_scene(nr_scene* s) {
     }
 }
 
-void finish_scene(nr_scene* s) {
+void finish_scene(nr_scene* s, const char* options) {
+    const nr::Config opt(options ? options : "");
+    const std::string bvh = opt.get_str("bvh");
+    if (!bvh.empty() && bvh != "host" && bvh != "gpu") throw NrError(NR_ERR_INVALID, "bvh must be host or gpu");
     NR_CUDA(cudaGetDevice(&s->device));
     NR_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device));
     NR_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     NR_CUDA(cudaMallocHost(&s->counters_host, nr::NUM_COUNTERS * sizeof(uint32_t)));
-    int threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    nr::build_bvh(s->host, s->bvh, threads);
+    auto t0 = std::chrono::steady_clock::now();
+    s->bvh_device_ms = 0.0;
+    if (bvh == "gpu") {
+        std::string err = nr::build_bvh_gpu(s->host.pos.data(), s->host.num_tris(), s->bvh, s->stream, &s->bvh_device_ms);
+        if (!err.empty()) throw NrError(NR_ERR_CUDA, err);
+    } else {
+        int threads = (int)std::max(1u, std::thread::hardware_concurrency());
+        nr::build_bvh(s->host, s->bvh, threads);
+    }
+    s->bvh_wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (s->bvh.max_depth + 2 > NR_STACK_LIMIT)
         throw NrError(NR_ERR_INVALID, "BVH depth " + std::to_string(s->bvh.max_depth) + " exceeds the traversal stack");
     nr::launch_setup(s->num_sms);
@@ -620,27 +633,39 @@ int nr_last_error(char* buf, size_t len) {
     return NR_OK;
 }
 
-int nr_scene_create(const nr_scene_desc* desc, nr_scene** out) {
+int nr_scene_create_opts(const nr_scene_desc* desc, const char* options, nr_scene** out) {
     return guarded([&]() {
         if (!desc || !out) throw NrError(NR_ERR_INVALID, "null argument");
         *out = nullptr;
         auto s = std::make_unique<nr_scene>();
         std::string err = nr::scene_from_desc(*desc, s->host);
         if (!err.empty()) throw NrError(NR_ERR_INVALID, err);
-        finish_scene(s.get());
+        finish_scene(s.get(), options);
         *out = s.release();
     });
 }
 
-int nr_scene_load(const char* text, nr_scene** out) {
+int nr_scene_create(const nr_scene_desc* desc, nr_scene** out) { return nr_scene_create_opts(desc, nullptr, out); }
+
+int nr_scene_load_opts(const char* text, const char* options, nr_scene** out) {
     return guarded([&]() {
         if (!text || !out) throw NrError(NR_ERR_INVALID, "null argument");
         *out = nullptr;
         auto s = std::make_unique<nr_scene>();
         std::string err = nr::scene_from_text(text, s->host);
         if (!err.empty()) throw NrError(err.rfind("cannot open", 0) == 0 ? NR_ERR_IO : NR_ERR_INVALID, err);
-        finish_scene(s.get());
+        finish_scene(s.get(), options);
         *out = s.release();
+    });
+}
+
+int nr_scene_load(const char* text, nr_scene** out) { return nr_scene_load_opts(text, nullptr, out); }
+
+int nr_scene_build_times(const nr_scene* s, double* bvh_wall_ms, double* bvh_device_ms) {
+    return guarded([&]() {
+        if (!s) throw NrError(NR_ERR_INVALID, "null scene");
+        if (bvh_wall_ms) *bvh_wall_ms = s->bvh_wall_ms;
+        if (bvh_device_ms) *bvh_device_ms = s->bvh_device_ms;
     });
 }
 

@@ -102,12 +102,16 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // refilled idle lanes from the queue with separate node and leaf phases,
 // 28 % slower; a four-wide tree collapsed from this one, no faster.)
 // Minimum resident 128-thread blocks per SM requested from the register
-// allocator for the two traversal kernels (occupancy against registers).
+// allocator for the two traversal kernels: 10 caps them at 48 registers
+// (40 warps per SM). Traversal is bound by dependent L2 latency, so the
+// extra warps pay: measured on GB300 for the 1M-triangle frame, 566
+// Mpaths/s at 10 against 530 with no cap (53 registers, 36 warps) and 541
+// at 12 (40 registers, with spills).
 #ifndef NR_TRACE_MINB
-#define NR_TRACE_MINB 1
+#define NR_TRACE_MINB 10
 #endif
 #ifndef NR_SHADOW_MINB
-#define NR_SHADOW_MINB 1
+#define NR_SHADOW_MINB 10
 #endif
 
 template <bool COUNT, bool FAST>

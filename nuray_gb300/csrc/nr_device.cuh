@@ -280,7 +280,7 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
             if (h1) { ref = k.y; continue; }
         } else {
             int first = leaf_first(ref), cnt = leaf_count(ref);
-            float lt = 1e18f, lb1 = 0.f, lb2 = 0.f;
+            float lt = 1e18f;
             int li = -1;
             for (int i = 0; i < cnt; ++i) {
                 int ti = first + i;
@@ -288,11 +288,11 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
                 ++nt;
                 float t, u, v;
                 if (FAST ? tri_test_fast(o, d, g0, g1, g2, lt, t, u, v) : tri_test(o, d, g0, g1, g2, lt, t, u, v)) {
-                    lt = t; lb1 = u; lb2 = v; li = ti;
+                    lt = t; li = ti;
                 }
             }
             if (li >= 0 && (lt < best_t || (lt == best_t && first > best_leaf))) {
-                best_t = lt; best_b1 = lb1; best_b2 = lb2; best = li; best_leaf = first;
+                best_t = lt; best = li; best_leaf = first;
             }
         }
         // pop the next subtree that can still hold a hit
@@ -305,6 +305,14 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
     }
     if (nodes_visited) *nodes_visited += nv;
     if (tris_tested) *tris_tested += nt;
+    if (best >= 0) {
+        // barycentrics of the winner, recomputed rather than carried through
+        // the loop (fewer live registers): both tests return the correctly
+        // rounded quotients, so these equal the values found in the leaf
+        float4 g0 = __ldg(&S.tri_geo[3 * best]), g1 = __ldg(&S.tri_geo[3 * best + 1]), g2 = __ldg(&S.tri_geo[3 * best + 2]);
+        float t;
+        tri_test(o, d, g0, g1, g2, 3.0e38f, t, best_b1, best_b2);
+    }
     return best;
 }
 
