@@ -249,6 +249,12 @@ def main():
     S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"], textures=sc["textures"],
                           env_tex=sc["env_tex"], env_gain=sc["env_gain"])
     build_s = time.perf_counter() - t0
+    bvh_host_ms = S.build_times()[0]
+    # the same tree built on the device (setup only; the timed steps use S)
+    G = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"], options="bvh=gpu")
+    bvh_gpu_wall_ms, bvh_gpu_dev_ms = G.build_times()
+    G.close()
+    del G
     stream = torch.cuda.ExternalStream(S.stream())
     cache = None
     if args.nrc is not None:
@@ -348,7 +354,9 @@ def main():
            "config": {"workload": desc, "triangles": int(sc["pos"].shape[0]), "paths_per_step": w * h * spp,
                       "l2": "inputs larger than L2 (scene ~150 MB, path state ~5.8 GB per batch); no flush",
                       "parallelism": f"{world} rank(s), disjoint sample ranges, no collective on the data path",
-                      "scene_build_s": round(build_s, 2)},
+                      "scene_build_s": round(build_s, 2),
+                      "bvh_build_ms": {"host_threads": round(bvh_host_ms, 1), "gpu_wall": round(bvh_gpu_wall_ms, 1),
+                                       "gpu_device": round(bvh_gpu_dev_ms, 1)}},
            "rays_per_s": round((rays + shadow_rays) / (ms / 1e3), 1), "extension_rays": rays,
            "shadow_rays": shadow_rays, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
            "e2e": e2e, "clocks": clk.summary()}

@@ -1,8 +1,11 @@
 """Builds libnuray_gpu.so in-tree (nuray_gb300/_build/) with nvcc for sm_103a.
 
-Three translation units compiled in parallel: the CUDA kernels
-(integrator.cu) and the host C++ (host_scene.cpp, capi.cpp), linked with
-nvcc into one shared library whose only interface is include/nuray.h.
+Every translation unit of csrc/ compiled in parallel (CUDA kernels with
+nvcc, host C++ with g++), linked with nvcc into one shared library whose
+only interface is include/nuray.h. Host code is compiled with
+-ffp-contract=off: g++ otherwise fuses a*b + c into FMAs for C++ on
+aarch64, and the host arithmetic that must reproduce the reference (SAH
+costs, camera, emitter areas) would round differently from x86.
 """
 import os
 import subprocess
@@ -61,10 +64,10 @@ def build(force=False, verbose=False):
         src = os.path.join(CSRC, f)
         obj = os.path.join(OUT, f + ".o")
         if f.endswith(".cu"):
-            jobs.append((obj, [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            jobs.append((obj, [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                                "-Xptxas", "-v" if verbose else "-O3", *inc, "-c", src, "-o", obj]))
         elif f.endswith(".cpp"):
-            jobs.append((obj, ["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
+            jobs.append((obj, ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
                                *inc, *cuda_inc, "-c", src, "-o", obj]))
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(lambda j: _run(j[1]), jobs))
@@ -75,7 +78,7 @@ def build(force=False, verbose=False):
     _run([_nvcc(), *ARCH, "-shared", "-o", tmp, *[j[0] for j in jobs], "-lpthread"])
     os.replace(tmp, LIB)
     # the command-line front end, linked against the library
-    _run(["g++", "-O2", "-std=c++17", *inc, os.path.join(CSRC, "cli", "nuray_main.cpp"), "-o", CLI,
+    _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", *inc, os.path.join(CSRC, "cli", "nuray_main.cpp"), "-o", CLI,
           "-L", OUT, "-lnuray_gpu", "-Wl,-rpath,$ORIGIN", "-lpthread"])
     return LIB
 

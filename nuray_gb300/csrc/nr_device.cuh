@@ -246,8 +246,8 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
     SlabRay R = make_slab_ray(o, d);
     float te;
     if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return -1;
-    int stack[NR_STACK];
-    float stack_t[NR_STACK];
+    // (subtree reference, entry distance) pairs: one 8-byte local access per push / pop
+    int2 stack[NR_STACK];
     int sp = 0;
     int ref = S.root_ref;
     uint32_t nv = 0, nt = 0;
@@ -272,7 +272,7 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
                 float ft = t1;
                 if (t1 < t0) { nr = k.y; fr = k.x; ft = t0; }
                 if (sp >= NR_STACK) { atomicOr(err, 1u); break; }
-                stack[sp] = fr; stack_t[sp] = ft; ++sp;
+                stack[sp] = make_int2(fr, __float_as_int(ft)); ++sp;
                 ref = nr;
                 continue;
             }
@@ -299,7 +299,8 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
         bool found = false;
         while (sp > 0) {
             --sp;
-            if (stack_t[sp] <= best_t * (1.0f + NR_PRUNE_MARGIN)) { ref = stack[sp]; found = true; break; }
+            const int2 e = stack[sp];
+            if (__int_as_float(e.y) <= best_t * (1.0f + NR_PRUNE_MARGIN)) { ref = e.x; found = true; break; }
         }
         if (!found) break;
     }

@@ -575,6 +575,11 @@ struct Policy {
     bool mis = true;
     int rrdepth = 0;   // RR applies from this vertex index on (0: every vertex, as the reference)
     int maxdepth = 0;  // 0: unbounded (the reference); else vertices 0..maxdepth-1 only
+    // renderer=nrc (RendererNRC::trace, src/renderer/renderernrc.cpp:13-185) with
+    // the cache never reached (path_lim beyond every path): light samples
+    // without MIS, an emitter hit counts only when the previous vertex took
+    // no light sample, and a path continues while u < prr
+    bool excl = false;
 };
 
 struct Counters { uint64_t rays = 0, shadow = 0, verts = 0; };
@@ -586,6 +591,13 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
     if (hit.tri < 0) {
         if (S.env < 0) return V3(0.f);
         // src/renderer/rendererptls.cpp:24-26, src/scene/envmap.cpp:17-24
+        if (P.excl) {
+            // renderernrc.cpp:24-25: renderernrc.h's `using namespace std` makes
+            // acos / atan2 of a float the float overloads there
+            float v = (float)(1 - (double)std::acos(dir.y) / PI_D);
+            float u = (float)((double)(std::atan2(dir.z, dir.x) / 2) / PI_D + 0.5);
+            return S.texs[S.env].uv(u, v) * S.env_gain;
+        }
         float v = (float)(1 - std::acos((double)dir.y) / PI_D);
         float u = (float)(std::atan2((double)dir.z, (double)dir.x) / 2 / PI_D + 0.5);
         return S.texs[S.env].uv(u, v) * S.env_gain;
@@ -602,6 +614,7 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
     V3 result;
     float fac = 1.0f;
     if (P.nee && mat_nee(M)) {
+        if (P.excl) fac = 0.0f;  // is_light_sampled (renderernrc.cpp:139)
         int li = S.lights.pick(smp);
         if (li >= 0) {
             const Tri& LT = S.tris[li];
@@ -619,7 +632,8 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
             float brdf_omega_pdf = mat_pdf(M, wo, normal, wl);
             float mis = light_omega_pdf / (light_omega_pdf + brdf_omega_pdf);
             if (!P.mis) mis = 0.5f;
-            fac = 1 - mis;
+            if (P.excl) mis = 1.0f;  // renderernrc.cpp:155: no MIS weight
+            else fac = 1 - mis;
             C.shadow++;
             BVH::Hit sh = S.bvh.intersect(hit_pos + wl * 1e-3f, wl);
             if ((double)sh.t + 2e-3 > (double)norm(light_vec)) {
@@ -633,7 +647,7 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
     // Russian roulette (src/renderer/rendererptls.cpp:80-83)
     float prr = depth < P.rrdepth ? 1.0f : P.prr;
     float rr = smp.random();
-    if (depth >= P.rrdepth && rr > prr) return result;
+    if (depth >= P.rrdepth && (P.excl ? !(rr < prr) : rr > prr)) return result;  // renderernrc.cpp:162: continue iff u < prr
     V3 wi = mat_sample(M, smp, wo, normal);
     float pdf = mat_pdf(M, wo, normal, wi);
     V3 brdf = mat_bxdf(M, wo, normal, wi, uv);
@@ -759,9 +773,12 @@ void port_render_samples(void* s, const char* params, int npix, const int* pix_x
     P.mis = c.i("mis", 1) != 0;
     P.rrdepth = c.i("rrdepth", 0);
     P.maxdepth = c.i("maxdepth", 0);
+    bool coin = false;
     {
         auto it = c.mp.find("renderer");
         P.nee = !(it != c.mp.end() && it->second == "pt");
+        P.excl = it != c.mp.end() && it->second == "nrc";
+        coin = P.excl;
     }
     int w = c.i("imgw", 1), h = c.i("imgh", 1);
     int nth = threads < 1 ? 1 : threads;
@@ -773,6 +790,7 @@ void port_render_samples(void* s, const char* params, int npix, const int* pix_x
             float jx = smp.random();
             float jy = smp.random();
             V3 dir = cam.ray((float)x + jx, (float)y + jy, (float)w, (float)h);
+            if (coin) (void)smp.random();  // RendererNRC::render's training coin (renderernrc.cpp:255)
             V3 L = trace(*S, P, smp, cam.pos, dir, 1.0f, 0, C[tid]);
             L = vmax(V3(0.0f), L);  // max(0.0f, trace(...)) (rendererptls.cpp:173)
             float* o = out + ((size_t)p * spp + i) * 3;

@@ -22,6 +22,7 @@
 //  * the reference Material virtuals on caller-given directions.
 #include "../renderer/rendererptls.h"
 #include "../renderer/rendererpt.h"
+#include "../renderer/renderernrc.h"
 #include "../scene/loader.h"
 #include "../material/matlambert.h"
 #include "../material/matggxrefl.h"
@@ -32,6 +33,7 @@
 #include "philox.h"
 
 #include <atomic>
+#include <memory>
 #include <thread>
 
 namespace {
@@ -60,6 +62,11 @@ public:
     using RendererPT::trace;
 };
 
+class OracleNRC : public RendererNRC {
+public:
+    using RendererNRC::trace;
+};
+
 class OracleRenderer : public RendererPTLS {
 public:
     using RendererPTLS::trace;
@@ -80,6 +87,8 @@ struct RefScene {
     std::vector<int> tri_mat;                   // per triangle index into mats
     OracleRenderer renderer;
     OraclePT plain;
+    OracleNRC nrc_renderer;
+    std::unique_ptr<NeuralRadianceCache> nrc;  // RendererNRC::render's cache, shape [64, 64, 64, 64, 3]
     Texture* env_tex = nullptr;
     Envmap* env = nullptr;
     ~RefScene() {
@@ -303,8 +312,10 @@ void ref_render_samples(void* h, const char* params, int npix, const int* pix_xy
     Camera cam = make_camera(config);
     int w = config.getValueInt("imgw", 1), hh = config.getValueInt("imgh", 1);
     std::streambuf* old = std::cerr.rdbuf(nullptr);  // getValueStr reports missing keys on stderr
-    const bool plain = config.getValueStr("renderer", "ptnee") == "pt";
+    const std::string rname = config.getValueStr("renderer", "ptnee");
+    const bool plain = rname == "pt", nrc_mode = rname == "nrc";
     std::cerr.rdbuf(old);
+    if (nrc_mode && !s->nrc) s->nrc = std::make_unique<NeuralRadianceCache>(std::vector<int>{64, 64, 64, 64, 3});
     parallel_for(npix, threads, [&](int p) {
         int x = pix_xy[2 * p], y = pix_xy[2 * p + 1];
         Config local = config;  // getValue* builds stringstreams; keep threads apart
@@ -313,10 +324,19 @@ void ref_render_samples(void* h, const char* params, int npix, const int* pix_xy
             float jx = smp.random();
             float jy = smp.random();
             vec3 ray_dir = cam.generateRay(x + jx, y + jy, w, hh);
-            vec3 L = plain ? max(0.0f, s->plain.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
-                                                      s->renderer.bvh(), s->env))
-                           : max(0.0f, s->renderer.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
-                                                         s->renderer.bvh(), true, s->env));
+            vec3 L;
+            if (nrc_mode) {
+                // RendererNRC::render (src/renderer/renderernrc.cpp:250-255): the
+                // training coin follows the jitter; no training here
+                (void)smp.random();
+                L = max(0.0f, s->nrc_renderer.trace(local, *s->nrc, 0, false, smp, cam.pos, ray_dir, *s->tris,
+                                                    s->renderer.lights(), s->renderer.bvh(), true, s->env));
+            } else {
+                L = plain ? max(0.0f, s->plain.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
+                                                     s->renderer.bvh(), s->env))
+                          : max(0.0f, s->renderer.trace(local, smp, cam.pos, ray_dir, *s->tris, s->renderer.lights(),
+                                                        s->renderer.bvh(), true, s->env));
+            }
             float* o = out + ((size_t)p * spp + i) * 3;
             o[0] = L[0]; o[1] = L[1]; o[2] = L[2];
         }

@@ -18,7 +18,7 @@ def load():
                    os.path.join(ROOT, "include", "nuray.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(p) > os.path.getmtime(LIB) for p in deps):
         os.makedirs(OUT, exist_ok=True)
-        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", CSRC, "-I",
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-shared", "-I", CSRC, "-I",
                         os.path.join(ROOT, "include"), *srcs, "-o", LIB, "-lpthread"], check=True)
     L = ctypes.CDLL(LIB)
     vp = ctypes.c_void_p

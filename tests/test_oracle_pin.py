@@ -176,3 +176,29 @@ def test_port_equals_reference_no_lights_and_empty(port_lib, ref_lib):
     P, R = Oracle("port", tiny), Oracle("ref", tiny)
     for a, b in zip(P.bvh(), R.bvh()):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_port_equals_reference_nrc_estimator(port_lib, ref_lib, seed):
+    """renderer=nrc: RendererNRC::trace (src/renderer/renderernrc.cpp:13-185)
+    with path_lim beyond every path, so its cache is never reached: light
+    samples without MIS, emitter hits dropped after a light sample, RR while
+    u < prr, and the training coin drawn after the jitter (:255)."""
+    sc = scenes.small_scene(seed)
+    P, R = Oracle("port", sc), Oracle("ref", sc)
+    params = sc["params"].replace("renderer=ptnee", "renderer=nrc") + " path_lim=1000000"
+    pix = pixel_grid(48, 32)
+    a, b = P.render_samples(params, pix, 4, seed=seed), R.render_samples(params, pix, 4, seed=seed)
+    np.testing.assert_array_equal(a, b)
+    ptls = P.render_samples(sc["params"], pix, 4, seed=seed)
+    assert not np.array_equal(a, ptls)  # a different estimator
+
+
+def test_port_equals_reference_nrc_estimator_cornell(port_lib, ref_lib):
+    import os
+    R = Oracle("ref", desc=os.path.join("/root/reference/scenes/cornell/CornellBox-Original.obj") + " -s 100\n")
+    P = Oracle("port", cornell_scene())
+    params = ("renderer=nrc imgw=80 imgh=60 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333 "
+              "path_lim=1000000")
+    pix = pixel_grid(80, 60)
+    np.testing.assert_array_equal(P.render_samples(params, pix, 4, seed=11), R.render_samples(params, pix, 4, seed=11))
