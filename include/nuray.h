@@ -221,8 +221,13 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
                          float* b2);
 
 /* Renders the image. params uses the reference grammar ("key=value ..."):
- * renderer (ptnee, the default, or pt: RendererPT, src/renderer/rendererpt.cpp:13-59,
- * the same estimator without light sampling), imgw imgh spp prr mis
+ * renderer (ptnee, the default; pt: RendererPT, src/renderer/rendererpt.cpp:13-59,
+ * the same estimator without light sampling; nrc: RendererNRC,
+ * src/renderer/renderernrc.cpp:13-281, light samples without MIS, a
+ * training coin per sample, one all-training first pass added to the image
+ * with the mean still divided by spp, and the attached cache asked from
+ * vertex path_lim (default 2) on, path_lim_train (default 4) on training
+ * paths; without an attached cache its estimator alone), imgw imgh spp prr mis
  * (reference keys and defaults) plus seed (Philox seed,
  * default 0), rrdepth (first vertex where Russian roulette applies, default 0
  * as in the reference), maxdepth (0 = unbounded as in the reference),

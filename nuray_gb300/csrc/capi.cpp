@@ -396,6 +396,7 @@ struct RenderArgs {
     float nrc_rough;  // roughness from which a GGX vertex is diffuse
     int nrc_direct;   // 1: light sample at the query vertex, cache for the rest
     int nrc_train_depth;  // > 0: training paths end in the cache from this depth on
+    bool nrc_pre;         // renderer=nrc: one all-training pass before the samples (RendererNRC::render)
 };
 
 RenderArgs parse_args(const nr_camera* cam, const char* params) {
@@ -414,11 +415,15 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
     a.pol.trav = c.get_int("trav", 1);
-    // renderer=ptnee (RendererPTLS) or pt (RendererPT, the same estimator without light sampling)
+    // renderer=ptnee (RendererPTLS), pt (RendererPT, the same estimator without
+    // light sampling) or nrc (RendererNRC: light samples without MIS, the
+    // cache asked from vertex path_lim on, path_lim_train on training paths)
     const std::string renderer = c.get_str("renderer");
+    a.pol.excl = a.pol.coin = a.pol.force_train = 0;
     if (renderer.empty() || renderer == "ptnee") a.pol.nee = 1;
     else if (renderer == "pt") a.pol.nee = 0;
-    else throw NrError(NR_ERR_INVALID, "renderer=" + renderer + " is not implemented (ptnee, pt)");
+    else if (renderer == "nrc") { a.pol.nee = 1; a.pol.excl = 1; a.pol.coin = 1; }
+    else throw NrError(NR_ERR_INVALID, "renderer=" + renderer + " is not implemented (ptnee, pt, nrc)");
     if (a.pol.trav < 0 || a.pol.trav > 1) throw NrError(NR_ERR_INVALID, "trav must be 0 or 1");
     a.wave = c.get_int("wave", 1 << 25);
     a.profile = c.get_int("profile", 0) != 0;
@@ -426,14 +431,16 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.sample0 = c.get_int("sample0", 0);
     a.accumulate = c.get_int("accumulate", 0) != 0;
     a.tile = c.get_int("tile", 1) != 0;
-    a.nrc = c.get_int("nrc", 0) != 0;
+    const bool nrc_mode = a.pol.excl != 0;
+    a.nrc = c.get_int("nrc", nrc_mode ? 1 : 0) != 0;
+    a.nrc_pre = nrc_mode && c.get_int("nrc_pre", 1) != 0;
     a.nrc_train = c.get_int("nrc_train", 16384);
     a.nrc_steps = c.get_int("nrc_steps", 2);
     a.nrc_query = c.get_int("nrc_query", 1);
-    a.nrc_mindepth = c.get_int("nrc_mindepth", 1);
+    a.nrc_mindepth = nrc_mode ? c.get_int("path_lim", 2) : c.get_int("nrc_mindepth", 1);
     a.nrc_rough = c.get_float("nrc_rough", 0.2f);
-    a.nrc_direct = c.get_int("nrc_direct", 1) != 0 ? 1 : 0;
-    a.nrc_train_depth = c.get_int("nrc_train_depth", 3);
+    a.nrc_direct = nrc_mode ? 0 : (c.get_int("nrc_direct", 1) != 0 ? 1 : 0);
+    a.nrc_train_depth = nrc_mode ? c.get_int("path_lim_train", 4) : c.get_int("nrc_train_depth", 3);
     if (a.nrc_train_depth < 0) throw NrError(NR_ERR_INVALID, "nrc_train_depth must be >= 0");
     if (a.nrc && (a.nrc_train <= 0 || a.nrc_steps <= 0)) throw NrError(NR_ERR_INVALID, "nrc_train and nrc_steps must be positive");
     if (a.sample0 < 0) throw NrError(NR_ERR_INVALID, "sample0 must be >= 0");
@@ -455,7 +462,9 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     const int cap = (int)std::min<uint64_t>(total, (uint64_t)A.wave);
     ensure_paths(s, cap);
     cudaStream_t st = s->stream;
-    const bool use_nrc = A.nrc;
+    // renderer=nrc without a cache attached renders its estimator alone (the
+    // reference with path_lim beyond every path)
+    const bool use_nrc = A.nrc && (s->nrc || !A.pol.excl);
     if (use_nrc) {
         if (!s->nrc) throw NrError(NR_ERR_INVALID, "nrc=1 needs a cache attached with nr_scene_attach_nrc");
         const int depth_cap = A.pol.maxdepth > 0 ? A.pol.maxdepth : 16;
@@ -726,6 +735,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         std::lock_guard<std::mutex> lk(s->mu);
         NR_CUDA(cudaSetDevice(s->device));
         RenderArgs A = parse_args(cam, params);
+        if (A.pol.excl) throw NrError(NR_ERR_INVALID, "the adjoint differentiates renderer=ptnee or pt");
         const int npix = A.pol.imgw * A.pol.imgh;
         const int nm = (int)s->host.mats.size();
         if ((size_t)nm * 7 * 4 > 200 * 1024) throw NrError(NR_ERR_INVALID, "too many materials for the adjoint (limit 7314)");
@@ -881,12 +891,26 @@ int nr_render(nr_scene* s, const nr_camera* cam, const char* params, float* hdr_
         const int npix = A.pol.imgw * A.pol.imgh;
         cudaStream_t st = s->stream;
         s->film.ensure((size_t)npix * sizeof(float4));
+        bool fresh = false;
         if (!A.accumulate || s->film_pixels != npix) {
             NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
             s->film_samples = 0;
             s->film_pixels = npix;
+            fresh = true;
         }
-        run_waves(s, A, npix, nullptr, A.sample0, s->film.as<float4>(), nullptr, cancel, progress, user);
+        int first = A.sample0;
+        if (A.nrc_pre && fresh) {
+            // RendererNRC::render (src/renderer/renderernrc.cpp:231-246): one
+            // pass in which every path trains, added to the image like the
+            // others, while the mean still divides by spp (:268)
+            RenderArgs P = A;
+            P.spp = 1;
+            P.pol.coin = 0;
+            P.pol.force_train = 1;
+            run_waves(s, P, npix, nullptr, first, s->film.as<float4>(), nullptr, cancel, nullptr, nullptr);
+            ++first;
+        }
+        run_waves(s, A, npix, nullptr, first, s->film.as<float4>(), nullptr, cancel, progress, user);
         s->film_samples += (uint64_t)A.spp;
         if (hdr_rgb || rgb8) {
             if (hdr_rgb) s->out_hdr.ensure((size_t)npix * 12);

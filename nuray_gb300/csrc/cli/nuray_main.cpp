@@ -6,9 +6,12 @@
 // e.g. nuray scenes/cornell/CornellBox-Original.obj -s 100 --output result.bmp
 //            --params renderer=ptnee imgw=320 imgh=240 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333
 //
-// renderer must be ptnee or pt (the reference also selects bdpt, pm, pssmlt
-// and nrc; those are not implemented here and are rejected). envmap= (PFM or binary
-// PPM) and envmap_gain= attach an environment map as the reference CLI does.
+// renderer must be ptnee, pt or nrc (the reference also selects bdpt, pm and
+// pssmlt; those are not implemented here and are rejected). For nrc a neural
+// radiance cache is created (learning rate from lr=, default 1e-3 as the
+// reference's SGD) and attached; path_lim= and path_lim_train= keep the
+// reference's meaning. envmap= (PNG, PFM or binary PPM) and envmap_gain=
+// attach an environment map as the reference CLI does.
 // The output is written by extension as PNG (8-bit RGB), BMP (24-bit, what
 // QImage::save produces for an RGB888 image), PPM (8-bit) or PFM (the linear
 // HDR mean); other extensions get BMP.
@@ -87,10 +90,11 @@ int main(int argc, char** argv) {
     }
     nr::Config cfg(params.str().c_str());
     std::string renderer = cfg.get_str("renderer");  // Config::getValueStr returns "" when absent
-    if (renderer != "ptnee" && renderer != "pt") {
-        std::cerr << "renderer=" << renderer << " is not available (this build implements renderer=ptnee and pt)\n";
+    if (renderer != "ptnee" && renderer != "pt" && renderer != "nrc") {
+        std::cerr << "renderer=" << renderer << " is not available (this build implements renderer=ptnee, pt and nrc)\n";
         return 2;
     }
+    nr_nrc* cache = nullptr;
     try {
         nr::RendererGPU r;
         r.prepare(scene_desc);
@@ -101,6 +105,11 @@ int main(int argc, char** argv) {
             std::string err = nr::read_image(env, w, h, rgb);
             if (!err.empty()) { std::cerr << err << "\n"; return 1; }
             nr::check(nr_scene_set_env(r.scene(), w, h, rgb.data(), cfg.get_float("envmap_gain", 1.0f)));
+        }
+        if (renderer == "nrc") {
+            const std::string opts = "lr=" + std::to_string(cfg.get_float("lr", 0.001f));
+            nr::check(nr_nrc_create(opts.c_str(), &cache));
+            nr::check(nr_scene_attach_nrc(r.scene(), cache));
         }
         nr::Image img;
         std::mutex mu;
@@ -115,8 +124,13 @@ int main(int argc, char** argv) {
             return 1;
         }
         std::cout << "finish:)" << std::endl;
+        if (cache) {
+            nr::check(nr_scene_attach_nrc(r.scene(), nullptr));
+            nr_nrc_destroy(cache);
+        }
     } catch (const nr::Error& e) {
         std::cerr << "error " << e.code << ": " << e.what() << "\n";
+        if (cache) nr_nrc_destroy(cache);
         return 1;
     }
     return 0;

@@ -73,11 +73,13 @@ __global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, P
     float jx = s.next();
     float jy = s.next();
     f3 d = camera_ray(cam, film_h, (float)x + jx, (float)y + jy, (float)pol.imgw, (float)pol.imgh);
+    uint32_t flags = pol.force_train ? NR_META_TRAIN : 0u;
+    if (pol.coin && (double)s.next() < 0.2) flags = NR_META_TRAIN;  // sampler.random() < 0.2 (renderernrc.cpp:255)
     P.ray_o[i] = make_float4(cam.pos[0], cam.pos[1], cam.pos[2], 0.f);
     P.ray_d[i] = make_float4(d.x, d.y, d.z, 0.f);
     P.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);
     P.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    P.meta[i] = make_uint4(key, sample, s.n, 0u);
+    P.meta[i] = make_uint4(key, sample, s.n, flags);
     P.queue_in[i] = i;
     if (i == 0) P.counters[CNT_IN] = (uint32_t)W.count;
 }
@@ -234,15 +236,18 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     float fac = 1.0f;
     const int depth = (int)(meta.w & NR_META_DEPTH_MASK);
     uint32_t flags = meta.w & NR_META_SEEN_DIFFUSE;
+    const uint32_t train_flag = meta.w & NR_META_TRAIN;
     bool query_here = false;
     int rec = -1;  // training record whose target leaves out this vertex's light sample
     if (NRC) {
-        const bool train = nrc_is_training(meta.x, meta.y, C.train_stride);
+        const bool train = pol.excl ? train_flag != 0 : nrc_is_training(meta.x, meta.y, C.train_stride);
         // Past the first diffuse bounce the cache stands in for the rest of the
         // path: from depth min_depth on, or for training paths from
         // train_depth on (their earlier vertices then learn from it).
+        // renderer=nrc asks at any vertex: depth >= path_lim, or
+        // path_lim_train on training paths (renderernrc.cpp:130).
         const bool end_here = train ? (C.train_depth > 0 && depth >= C.train_depth) : depth >= C.min_depth;
-        if (flags && C.query && end_here) {
+        if ((flags || pol.excl) && C.query && end_here) {
             int q = warp_append(true, &C.counters[0]);
             C.q_slot[q] = slot;
             C.q_thr[q] = make_float4(T.x, T.y, T.z, 0.f);
@@ -265,6 +270,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     }
 
     // next-event estimation (rendererptls.cpp:49-78)
+    if (pol.excl && pol.nee && mat_nee(type)) fac = 0.0f;  // is_light_sampled (renderernrc.cpp:139)
     if (pol.nee && mat_nee(type) && S.num_lights > 0) {
         float r = rng.next();
         // LightSampler::sampleLight: lower_bound over the CDF
@@ -293,7 +299,8 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
         float brdf_omega_pdf = mat_pdf(M, wo, normal, wl);
         float mis = light_omega_pdf / (light_omega_pdf + brdf_omega_pdf);
         if (!pol.mis) mis = 0.5f;
-        fac = 1.0f - mis;
+        if (pol.excl) mis = 1.0f;  // renderernrc.cpp:155: no MIS weight
+        else fac = 1.0f - mis;
         f3 brdf = mat_bxdf(M, wo, normal, wl);
         f3 Ll = Ke / norm2(light_vec) * smax(0.f, cos_l) / light_pdf;
         f3 c = Ll * brdf * smax(0.f, dot(normal, normalized(light_pos - hit_pos))) * mis;
@@ -324,7 +331,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     // Russian roulette (rendererptls.cpp:80-83)
     float prr = depth < pol.rrdepth ? 1.0f : pol.prr;
     float u = rng.next();
-    if (depth >= pol.rrdepth && u > prr) return;
+    if (depth >= pol.rrdepth && (pol.excl ? !(u < prr) : u > prr)) return;  // renderernrc.cpp:162: go on while u < prr
     f3 wi = mat_sample(M, rng, wo, normal);
     float pdf = mat_pdf(M, wo, normal, wi);
     f3 brdf = mat_bxdf(M, wo, normal, wi);
@@ -336,7 +343,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
     P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
     P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
-    P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, (uint32_t)(depth + 1) | flags);
+    P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, (uint32_t)(depth + 1) | flags | train_flag);
 }
 
 // Shades the bucketed queue: categories are contiguous, so each warp mostly

@@ -65,6 +65,10 @@ struct Policy {
     uint32_t seed_lo, seed_hi;
     int32_t imgw, imgh;
     int32_t nee;      // 1: ptnee (RendererPTLS); 0: pt (RendererPT), no light sampling
+    int32_t excl;     // 1: renderer=nrc's estimator (RendererNRC::trace): light samples without
+                      // MIS, emitter hits dropped after a light sample, paths go on while u < prr
+    int32_t coin;     // 1: a training coin is drawn after the jitter (RendererNRC::render)
+    int32_t force_train;  // 1: every path is a training path (RendererNRC::render's first pass)
     int32_t trav;     // traversal tests: 0 exact arithmetic only, 1 fast path with exact fallback (same hits)
 };
 
@@ -113,6 +117,7 @@ struct NrcCtx {
 // meta.w: vertex depth in the low 16 bits; this flag once a diffuse vertex
 // has been passed (NRC mode).
 #define NR_META_SEEN_DIFFUSE 0x80000000u
+#define NR_META_TRAIN 0x40000000u  // training path by coin or forced (renderer=nrc)
 #define NR_META_DEPTH_MASK 0xffffu
 
 // Shading categories for the material sort: one per material type, then

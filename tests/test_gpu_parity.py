@@ -127,7 +127,7 @@ def test_samples_mixed_same_stream(gpu_lib):
 
 
 @pytest.mark.parametrize("extra", ["rrdepth=3 maxdepth=8", "mis=0 prr=0.6", "maxdepth=2", "seed=12345678901",
-                                   "renderer=pt"])
+                                   "renderer=pt", "renderer=nrc path_lim=1000000"])
 def test_samples_policies_vs_port(gpu_lib, port_lib, extra):
     sc = cornell_scene()
     S, P = gpu_scene(sc), Oracle("port", sc)
@@ -221,10 +221,12 @@ def test_errors_and_cancel(gpu_lib):
         gpu_scene(dict(cornell_scene(), mat=np.full(36, 99, np.int32)))
 
 
-def test_env_miss_and_textures_vs_port(gpu_lib, port_lib):
+@pytest.mark.parametrize("renderer", ["ptnee", "nrc"])
+def test_env_miss_and_textures_vs_port(gpu_lib, port_lib, renderer):
     sc = scenes.small_scene(5)
     S, P = gpu_scene(sc), Oracle("port", sc)
     pix = pixel_grid(48, 32)
-    a = S.render_samples(sc["params"], pix, 4)
-    b = P.render_samples(sc["params"], pix, 4)
+    params = sc["params"].replace("renderer=ptnee", f"renderer={renderer}") + " path_lim=1000000"
+    a = S.render_samples(params, pix, 4)
+    b = P.render_samples(params, pix, 4)
     assert _sample_match(a, b) >= 0.97
