@@ -6,8 +6,9 @@ One step renders one full frame of the workload: the seeded 1M-triangle
 terrain + spheres scene, 1920x1080, 64 samples per pixel, max depth 8,
 Russian roulette from depth 3, Philox seed 0 (132.7 M camera paths). The
 scene (BVH, triangles, materials) and the path state live in HBM; both are
-larger than the 129 MB L2 (about 150 MB of scene and 5.8 GB of path state
-per wavefront batch of 2^25 paths), so no L2 flush is inserted between steps.
+larger than the 129 MB L2 (about 150 MB of scene and 24 GB of path state:
+the whole frame is one wavefront batch of up to 2^27 paths), so no L2
+flush is inserted between steps.
 
 value: paths / s with the scene resident and the image left on the device
 (nr_render with no host output), timed with CUDA events on the library's
@@ -47,7 +48,7 @@ BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry
 # DRAM bytes (read + write) per closest-hit ray of k_trace, from one ncu
 # capture of a bounce-0 launch (profiles/k_trace_c2_first_bounce.md); the
 # roofline's `traffic` scales it to a full launch by rays per launch.
-TRACE_DRAM_BYTES_PER_RAY = 117.8
+TRACE_DRAM_BYTES_PER_RAY = 122.5
 
 
 def parse():
@@ -341,6 +342,17 @@ def main():
     roof["traffic"] = round(TRACE_DRAM_BYTES_PER_RAY * rays / max(1, trace_launches))
     roof["traffic_note"] = ("ncu DRAM bytes per ray of a bounce-0 k_trace launch (small case of the same scene) "
                             "x rays per launch")
+    # the whole path's algorithmic bytes as SURVEY 8(d) defines them:
+    # sum over rays (32 B per node, 36 B per triangle) + 240 B per shaded
+    # vertex (hit attributes, material, path state, hit record) + 12 B film
+    paths1 = max(1, cnt["paths"])
+    b_path = ((32 * cnt["nodes_visited"] + 36 * cnt["tris_tested"] + 32 * cnt["shadow_nodes_visited"]
+               + 36 * cnt["shadow_tris_tested"]) / paths1 + 240 * cnt["rays"] / paths1 + 12)
+    path_gbs = value * 1e6 * b_path / 1e9
+    roof["path"] = {"bytes_per_path": round(b_path, 1), "achieved": round(path_gbs, 1),
+                    "frac": round(path_gbs / peak, 3),
+                    "formula": "sum_rays(32 N_node + 36 N_tri) + 240 per shaded vertex + 12, counts of an "
+                               "instrumented frame, x paths/s"}
 
     cpu = None
     if not args.no_cpu and world == 1:
@@ -352,7 +364,7 @@ def main():
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded procedural scene; the reference publishes no benchmark scene)",
            "config": {"workload": desc, "triangles": int(sc["pos"].shape[0]), "paths_per_step": w * h * spp,
-                      "l2": "inputs larger than L2 (scene ~150 MB, path state ~5.8 GB per batch); no flush",
+                      "l2": "inputs larger than L2 (scene ~150 MB, path state ~24 GB); no flush",
                       "parallelism": f"{world} rank(s), disjoint sample ranges, no collective on the data path",
                       "scene_build_s": round(build_s, 2),
                       "bvh_build_ms": {"host_threads": round(bvh_host_ms, 1), "gpu_wall": round(bvh_gpu_wall_ms, 1),

@@ -425,7 +425,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     else if (renderer == "nrc") { a.pol.nee = 1; a.pol.excl = 1; a.pol.coin = 1; }
     else throw NrError(NR_ERR_INVALID, "renderer=" + renderer + " is not implemented (ptnee, pt, nrc)");
     if (a.pol.trav < 0 || a.pol.trav > 1) throw NrError(NR_ERR_INVALID, "trav must be 0 or 1");
-    a.wave = c.get_int("wave", 1 << 25);
+    a.wave = c.get_int("wave", 1 << 27);
     a.profile = c.get_int("profile", 0) != 0;
     a.count = c.get_int("count", 0) != 0;
     a.sample0 = c.get_int("sample0", 0);
