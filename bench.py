@@ -68,9 +68,11 @@ def parse():
     ap.add_argument("--nrc", default=None, metavar="PARAMS",
                     help="each step is a PT + NRC frame: a fresh cache is attached and the render gets "
                          "'nrc=1 nrc_train=16384 PARAMS' (measures the cache's per-frame cost)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
                     help="c2: the 1M-triangle scene (default); c3: the same with an HDR sky, value-noise "
-                         "textures on half the materials and 10%% GGX dielectrics, spp 256")
+                         "textures on half the materials and 10%% GGX dielectrics, spp 256; c5: the path-replay "
+                         "adjoint on the 200k-triangle, 64-material inverse-rendering scene (512x512, spp 32, "
+                         "depth 4), one gradient per step")
     args = ap.parse_args()
     if args.nrc is not None:
         args.no_relmse = True  # the comparison attaches caches of its own
@@ -230,11 +232,67 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args, local):
+    """--workload c5: each step is one nr_adjoint call (primal replay, then
+    adjoint replay of every path) for a fixed seeded d loss / d image; the
+    per-material gradient comes back to the host inside the timed region."""
+    import torch
+    from nuray_gb300 import Scene, build, inverse
+    build.build()
+    sc = inverse.c5_scene(0)
+    S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"])
+    params = sc["params"]
+    w = h = 512
+    spp = 32
+    rng = np.random.default_rng(7)
+    dl = (rng.standard_normal((h, w, 3)) / (w * h * 3)).astype(np.float32)
+    S.render_device(params.replace("spp=32", "spp=1") + " count=1")
+    cnt = S.stats()
+    stream = torch.cuda.ExternalStream(S.stream())
+    for k in range(args.warmup):
+        S.adjoint(params + f" seed={k + 1}", dl)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for k in range(args.steps):
+            S.adjoint(params + f" seed={100 + k}", dl)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    paths = w * h * spp * args.steps
+    value = paths / (ms / 1e3) / 1e6
+    pk, pk_kind = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    paths1 = max(1, cnt["paths"])
+    b_path = ((32 * cnt["nodes_visited"] + 36 * cnt["tris_tested"] + 32 * cnt["shadow_nodes_visited"]
+               + 36 * cnt["shadow_tris_tested"]) / paths1 + 240 * cnt["rays"] / paths1 + 12)
+    achieved = 2 * b_path * paths / (ms / 1e3) / 1e9  # every path is traced twice
+    out = {"metric": "Mpaths/s adjoint", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 2),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded procedural scene, seeded d loss / d image)",
+           "config": {"workload": f"path-replay adjoint, {sc['pos'].shape[0]} triangles, {len(sc['mats'])} "
+                                  f"materials, {w}x{h}, spp={spp}, maxdepth 4, RR from depth 3",
+                      "paths_per_step": w * h * spp},
+           "roofline": {"kernel": "k_adjoint (primal + adjoint replay)", "bound": "hbm",
+                        "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 3), "peak_source": pk_kind, "traffic": None,
+                        "bytes_per_path": round(2 * b_path, 1)},
+           "gpu_launches": args.steps * S.stats()["kernel_launches"], "cpu_baseline": None, "e2e": None,
+           "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "c5":
+        if rank == 0:
+            run_adjoint(args, local)
         return
     import torch
     torch.cuda.set_device(local)
@@ -252,7 +310,8 @@ def main():
     build_s = time.perf_counter() - t0
     bvh_host_ms = S.build_times()[0]
     # the same tree built on the device (setup only; the timed steps use S)
-    G = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"], options="bvh=gpu")
+    G = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"], textures=sc["textures"],
+                          env_tex=sc["env_tex"], env_gain=sc["env_gain"], options="bvh=gpu")
     bvh_gpu_wall_ms, bvh_gpu_dev_ms = G.build_times()
     G.close()
     del G

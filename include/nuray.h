@@ -241,6 +241,9 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * their films sum), tile (1, the default: the paths of a wave are ordered by
  * 8x4 pixel tiles when imgw % 8 == 0 and imgh % 4 == 0, so a warp's camera
  * rays are coherent; 0: scanline order; the image is the same either way),
+ * envis=1 (ptnee only, no reference counterpart: one environment light
+ * sample per light-sampling vertex besides the area-light sample, weighted
+ * against BSDF-sampled misses by the balance heuristic; same expected image),
  * profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
  * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
  * (W*H*3 bytes: mean^(1/2.2)*255 clamped and truncated, as

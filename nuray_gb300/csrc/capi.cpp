@@ -117,6 +117,7 @@ struct nr_scene {
     nr::Bvh bvh;
     nr::DeviceScene dev{};
     DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_mat;
+    DevBuf env_weight, env_row_cdf, env_col_cdf;  // environment sampling table (envis=1)
     int num_gpu_nodes = 0;
     // wavefront state
     DevBuf path_mem, film, out_hdr, out_rgb8, pix_list, scratch;
@@ -124,6 +125,7 @@ struct nr_scene {
     uint64_t film_samples = 0;  // samples summed in film (accumulate=1 keeps adding)
     nr::PathState ps{};
     int capacity = 0;
+    int sh_mult = 1;  // shadow-ray queue entries per path slot
     uint32_t* counters_host = nullptr;  // pinned
     nr_stats stats{};
     std::vector<cudaEvent_t> ev_pool;  // profile=1: events around every kernel group
@@ -244,8 +246,10 @@ void upload_scene(nr_scene* s) {
     std::vector<float4> texels;
     std::vector<int4> tinfo;
     size_t off = 0;
+    nr::EnvTable env_table;
     for (size_t t = 0; t < H.tex_wh.size() / 2; ++t) {
         int w = H.tex_wh[2 * t], h = H.tex_wh[2 * t + 1];
+        if ((int)t == H.env_tex) nr::build_env_table(&H.tex_data[3 * off], w, h, env_table);
         tinfo.push_back(make_int4(w, h, (int)(off / 1), 0));
         for (size_t k = 0; k < (size_t)w * h; ++k) {
             const float* c = &H.tex_data[3 * (off + k)];
@@ -264,6 +268,9 @@ void upload_scene(nr_scene* s) {
     upload(s->lights, lt, st);
     upload(s->light_cdf, cdf, st);
     upload(s->light_mat, lmat, st);
+    upload(s->env_weight, env_table.weight, st);
+    upload(s->env_row_cdf, env_table.row_cdf, st);
+    upload(s->env_col_cdf, env_table.col_cdf, st);
     NR_CUDA(cudaStreamSynchronize(st));
 
     nr::DeviceScene& D = s->dev;
@@ -276,6 +283,10 @@ void upload_scene(nr_scene* s) {
     D.lights = s->lights.as<float4>();
     D.light_cdf = s->light_cdf.as<float>();
     D.light_mat = s->light_mat.as<int32_t>();
+    D.env_weight = env_table.w ? s->env_weight.as<float>() : nullptr;
+    D.env_row_cdf = env_table.w ? s->env_row_cdf.as<float>() : nullptr;
+    D.env_col_cdf = env_table.w ? s->env_col_cdf.as<float>() : nullptr;
+    D.env_total = env_table.total;
     D.num_lights = (int)pdf.size();
     D.light_p = (float)(1.0 / ((double)sum + 1e-8));
     D.num_tris = n;
@@ -318,11 +329,13 @@ void finish_scene(nr_scene* s, const char* options) {
 }
 
 // Sizes the path-state buffers for `cap` slots.
-void ensure_paths(nr_scene* s, int cap) {
-    if (cap <= s->capacity) return;
-    const size_t C = (size_t)cap;
+void ensure_paths(nr_scene* s, int cap, int sh_mult = 1) {
+    if (cap <= s->capacity && sh_mult <= s->sh_mult) return;
+    cap = std::max(cap, s->capacity);
+    sh_mult = std::max(sh_mult, s->sh_mult);
+    const size_t C = (size_t)cap, CS = C * (size_t)sh_mult;
     const size_t f4 = 16;
-    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 2 + C * 4 * nr::NUM_CAT + C * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
+    size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 2 + C * 4 * nr::NUM_CAT + CS * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
     s->path_mem.alloc(bytes);
     char* p = s->path_mem.as<char>();
     auto take = [&](size_t n) { char* r = p; p += (n + 255) & ~size_t(255); return r; };
@@ -336,12 +349,14 @@ void ensure_paths(nr_scene* s, int cap) {
     P.queue_in = (int32_t*)take(C * 4);
     P.queue_out = (int32_t*)take(C * 4);
     P.sorted = (int32_t*)take(C * 4 * nr::NUM_CAT);
-    P.sh_o = (float4*)take(C * f4);
-    P.sh_d = (float4*)take(C * f4);
-    P.sh_c = (float4*)take(C * f4);
+    P.sh_o = (float4*)take(CS * f4);
+    P.sh_d = (float4*)take(CS * f4);
+    P.sh_c = (float4*)take(CS * f4);
+    P.sh_cap = (int32_t)std::min<size_t>(CS, (size_t)INT32_MAX);
     P.counters = (uint32_t*)take(nr::NUM_COUNTERS * 4);
     NR_CUDA(cudaMemsetAsync(P.counters, 0, nr::NUM_COUNTERS * 4, s->stream));
     s->capacity = cap;
+    s->sh_mult = sh_mult;
 }
 
 // Sizes the batch scratch of a cache for m rows.
@@ -424,6 +439,9 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     else if (renderer == "pt") a.pol.nee = 0;
     else if (renderer == "nrc") { a.pol.nee = 1; a.pol.excl = 1; a.pol.coin = 1; }
     else throw NrError(NR_ERR_INVALID, "renderer=" + renderer + " is not implemented (ptnee, pt, nrc)");
+    a.pol.envis = c.get_int("envis", 0) != 0 ? 1 : 0;
+    if (a.pol.envis && (renderer == "pt" || renderer == "nrc"))
+        throw NrError(NR_ERR_INVALID, "envis applies to renderer=ptnee");
     if (a.pol.trav < 0 || a.pol.trav > 1) throw NrError(NR_ERR_INVALID, "trav must be 0 or 1");
     a.wave = c.get_int("wave", 1 << 27);
     a.profile = c.get_int("profile", 0) != 0;
@@ -460,7 +478,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                float* dev_out, volatile int32_t* cancel, void (*progress)(float, void*), void* user) {
     const uint64_t total = (uint64_t)npix * (uint64_t)A.spp;
     const int cap = (int)std::min<uint64_t>(total, (uint64_t)A.wave);
-    ensure_paths(s, cap);
+    ensure_paths(s, cap, A.pol.envis ? 2 : 1);
     cudaStream_t st = s->stream;
     // renderer=nrc without a cache attached renders its estimator alone (the
     // reference with path_lim beyond every path)
@@ -628,7 +646,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     }
     S.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (c[nr::CNT_ERR] != 0)
-        throw NrError(NR_ERR_DEVICE, "traversal error bits " + std::to_string(c[nr::CNT_ERR]) + " (1 stack overflow, 2 step cap)");
+        throw NrError(NR_ERR_DEVICE, "device error bits " + std::to_string(c[nr::CNT_ERR]) +
+                                         " (1 stack overflow, 2 step cap, 4 shadow queue full)");
 }
 
 }  // namespace
@@ -736,6 +755,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         NR_CUDA(cudaSetDevice(s->device));
         RenderArgs A = parse_args(cam, params);
         if (A.pol.excl) throw NrError(NR_ERR_INVALID, "the adjoint differentiates renderer=ptnee or pt");
+        if (A.pol.envis) throw NrError(NR_ERR_INVALID, "the adjoint does not support envis");
         const int npix = A.pol.imgw * A.pol.imgh;
         const int nm = (int)s->host.mats.size();
         if ((size_t)nm * 7 * 4 > 200 * 1024) throw NrError(NR_ERR_INVALID, "too many materials for the adjoint (limit 7314)");
@@ -772,6 +792,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         if (image) for (size_t i = 0; i < (size_t)npix * 3; ++i) image[i] /= (float)A.spp;
         s->stats = nr_stats{};
         s->stats.paths = (uint64_t)npix * A.spp;
+        s->stats.kernel_launches = 1;  // k_adjoint
         s->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }

@@ -210,6 +210,48 @@ std::string read_image(const std::string& path, int& w, int& h, std::vector<floa
     return "unsupported image format (PNG, PFM or binary PPM): " + path;
 }
 
+void build_env_table(const float* rgb, int w, int h, EnvTable& T) {
+    T = EnvTable{};
+    if (w <= 0 || h <= 0) return;
+    T.w = w;
+    T.h = h;
+    T.weight.assign((size_t)w * h, 0.f);
+    T.row_cdf.assign((size_t)h, 0.f);
+    T.col_cdf.assign((size_t)w * h, 0.f);
+    auto lum = [&](int x, int y) -> float {
+        if (x >= w || y >= h) return 0.f;
+        const float* c = rgb + 3 * ((size_t)y * w + x);
+        return c[0] + c[1] + c[2];
+    };
+    std::vector<float> row_sum((size_t)h, 0.f);
+    for (int y = 0; y < h; ++y) {
+        const float th = ((float)y + 0.5f) / (float)h * 3.14159f;
+        const float sn = std::sin(th);
+        float acc = 0.f;
+        for (int x = 0; x < w; ++x) {
+            float m = std::max(std::max(lum(x, y), lum(x + 1, y)), std::max(lum(x, y + 1), lum(x + 1, y + 1)));
+            float wt = m > 0.f ? m * sn : 0.f;
+            T.weight[(size_t)y * w + x] = wt;
+            acc += wt;
+            T.col_cdf[(size_t)y * w + x] = acc;
+        }
+        row_sum[y] = acc;
+        for (int x = 0; x < w; ++x) {
+            float& c = T.col_cdf[(size_t)y * w + x];
+            c = acc > 0.f ? c / acc : (float)(x + 1) / (float)w;
+        }
+        T.col_cdf[(size_t)y * w + w - 1] = 1.f;
+    }
+    float acc = 0.f;
+    for (int y = 0; y < h; ++y) {
+        acc += row_sum[y];
+        T.row_cdf[y] = acc;
+    }
+    T.total = acc;
+    for (int y = 0; y < h; ++y) T.row_cdf[y] = acc > 0.f ? T.row_cdf[y] / acc : (float)(y + 1) / (float)h;
+    T.row_cdf[h - 1] = 1.f;
+}
+
 // ------------------------------------------------------------------ OBJ / MTL
 namespace {
 

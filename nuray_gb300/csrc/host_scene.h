@@ -62,6 +62,23 @@ std::string scene_from_text(const std::string& desc, HostScene& out);
 // the top.
 std::string read_image(const std::string& path, int& w, int& h, std::vector<float>& rgb);
 
+// Sampling table of an environment map for envis=1 (no counterpart in the
+// reference, whose ptnee only looks the map up on a miss). Cell (x, y) is
+// the square between texels (x, y) and (x + 1, y + 1) over which the
+// bilinear lookup interpolates (texels past the right / bottom edge are
+// black, as Texture::pixel makes them). Its weight is the largest r + g + b
+// of its four corners times sin(theta) at the cell's centre row, theta =
+// (y + 0.5) / h * 3.14159; rows and columns are drawn from cumulative sums
+// (float, in index order, the last entry forced to 1).
+struct EnvTable {
+    int w = 0, h = 0;
+    std::vector<float> weight;   // w * h
+    std::vector<float> row_cdf;  // h
+    std::vector<float> col_cdf;  // w * h, per row
+    float total = 0.f;
+};
+void build_env_table(const float* rgb, int w, int h, EnvTable& out);
+
 // Binary BVH with the reference's SAH (BVH::_divide, src/hierarchy/bvh.cpp:5-58):
 // primitives sorted by pMax along each axis, prefix/suffix surface-area sweep
 // with cost SA_L * |L| + SA_R * (|R| + 1), leaves of at most 5 triangles.

@@ -191,19 +191,45 @@ __device__ __forceinline__ bool nrc_is_training(uint32_t pixel, uint32_t sample,
     return hash32(pixel ^ hash32(sample + 0x9e3779b9u)) % stride == 0u;
 }
 
+// Queues a shadow ray (or, when no hit can come before the limit, adds its
+// contribution at once). rec: the training record whose target leaves this
+// light sample out, or -1.
+template <bool NRC>
+__device__ __forceinline__ void emit_shadow(const PathState& P, const NrcCtx& C, int slot, int rec, f3 so, f3 d,
+                                            float tmax, f3 c) {
+    if (tmax > 0.f) {
+        int q = warp_append(true, &P.counters[CNT_SHADOW]);
+        if (q >= P.sh_cap) { atomicOr(&P.counters[CNT_ERR], 4u); return; }
+        P.sh_o[q] = make_float4(so.x, so.y, so.z, tmax);
+        P.sh_d[q] = make_float4(d.x, d.y, d.z, __int_as_float(slot));
+        P.sh_c[q] = make_float4(c.x, c.y, c.z, __int_as_float(rec));
+    } else {
+        float4 r = P.rad[slot];
+        P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+        if (NRC && rec >= 0) {
+            float4 b = C.t_before[rec];
+            C.t_before[rec] = make_float4(b.x + c.x, b.y + c.y, b.z + c.z, 0.f);
+        }
+    }
+}
+
 template <bool NRC>
 __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
                                           const NrcCtx& C) {
     float4 h = P.hit[slot];
     float4 thr = P.thr[slot];
     uint4 meta = P.meta[slot];
-    f3 dir = xyz(P.ray_d[slot]);
+    const float4 dir4 = P.ray_d[slot];
+    f3 dir = xyz(dir4);
     f3 T = xyz(thr);
     int tri = __float_as_int(h.w);
     if (tri < 0) {
         if (S.env_tex >= 0) {
             float4 r = P.rad[slot];
             f3 e = env_lookup(S, dir);
+            // envis: the previous vertex also sampled the environment; dir4.w
+            // holds the BSDF density of this direction (balance heuristic)
+            if (dir4.w > 0.f && S.env_weight) e = e * (dir4.w / (dir4.w + env_pdf(S, dir)));
             P.rad[slot] = make_float4(r.x + T.x * e.x, r.y + T.y * e.y, r.z + T.z * e.z, 0.f);
         }
         return;
@@ -310,19 +336,27 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
             // double there), i.e. occluded iff some hit has t <= |lv| - 2e-3.
             double lim = (double)norm(light_vec) - 2e-3;
             float tmax = lim > 0.0 ? __double2float_rd(lim) : 0.0f;
-            if (tmax > 0.f) {
-                int q = warp_append(true, &P.counters[CNT_SHADOW]);
-                f3 so = hit_pos + wl * 1e-3f;
-                P.sh_o[q] = make_float4(so.x, so.y, so.z, tmax);
-                P.sh_d[q] = make_float4(wl.x, wl.y, wl.z, __int_as_float(slot));
-                P.sh_c[q] = make_float4(c.x, c.y, c.z, __int_as_float(rec));
-            } else {  // no hit with t > 0 can be that close: always visible
-                float4 r = P.rad[slot];
-                P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
-                if (NRC && rec >= 0) {
-                    float4 b = C.t_before[rec];
-                    C.t_before[rec] = make_float4(b.x + c.x, b.y + c.y, b.z + c.z, 0.f);
-                }
+            emit_shadow<NRC>(P, C, slot, rec, hit_pos + wl * 1e-3f, wl, tmax, c);
+        }
+    }
+    // envis: one environment light sample more (no counterpart in the
+    // reference), weighted against the BSDF-sampled miss by the balance
+    // heuristic; its two draws follow the area-light draws
+    bool env_sampled = false;
+    if (pol.envis && pol.nee && mat_nee(type) && S.env_weight) {
+        env_sampled = true;
+        const float r1 = rng.next(), r2 = rng.next();
+        f3 we;
+        float pe;
+        if (env_sample(S, r1, r2, we, pe)) {
+            const float cosn = dot(normal, we);
+            if (cosn > 0.f) {
+                // at the depth limit no BSDF sample follows: the light sample takes the full weight
+                const bool last = pol.maxdepth > 0 && depth + 1 >= pol.maxdepth;
+                const float pb = last ? 0.f : mat_pdf(M, wo, normal, we);
+                const f3 c = T * mat_bxdf(M, wo, normal, we) * env_lookup(S, we) * (cosn / (pe + pb));
+                if (c.x != 0.f || c.y != 0.f || c.z != 0.f)
+                    emit_shadow<NRC>(P, C, slot, rec, hit_pos + we * 1e-3f, we, 3.0e38f, c);
             }
         }
     }
@@ -341,7 +375,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     int q = warp_append(true, &P.counters[CNT_OUT]);
     P.queue_out[q] = slot;
     P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
-    P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
+    P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, env_sampled ? pdf : 0.f);
     P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
     P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, (uint32_t)(depth + 1) | flags | train_flag);
 }

@@ -39,6 +39,56 @@ __device__ __forceinline__ f3 env_lookup(const DeviceScene& S, f3 dir) {
     return tex_uv(S, S.env_tex, u, v) * S.env_gain;
 }
 
+// Environment light sampling (envis=1; no counterpart in the reference):
+// a cell of the sampling table by its row and column CDFs, a uniform point
+// in the cell, the direction env_lookup maps that point from, and the
+// solid-angle density, table density * w * h / (2 pi^2 sin theta) (with
+// the reference's pi of 3.14159, the one the lookup uses).
+__device__ __forceinline__ int cdf_upper(const float* cdf, int n, float r) {  // first i with cdf[i] > r
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(&cdf[mid]) > r) hi = mid; else lo = mid + 1;
+    }
+    return lo < n ? lo : n - 1;
+}
+__device__ __forceinline__ bool env_sample(const DeviceScene& S, float r1, float r2, f3& dir, float& pdf) {
+    const int4 info = __ldg(&S.tex_info[S.env_tex]);
+    const int w = info.x, h = info.y;
+    const int y = cdf_upper(S.env_row_cdf, h, r1);
+    const float c0 = y ? __ldg(&S.env_row_cdf[y - 1]) : 0.f, c1 = __ldg(&S.env_row_cdf[y]);
+    const float fy = fminf(fmaxf(c1 > c0 ? (r1 - c0) / (c1 - c0) : 0.5f, 0.f), 0.99999994f);
+    const float* col = S.env_col_cdf + (size_t)y * w;
+    const int x = cdf_upper(col, w, r2);
+    const float d0 = x ? __ldg(&col[x - 1]) : 0.f, d1 = __ldg(&col[x]);
+    const float fx = fminf(fmaxf(d1 > d0 ? (r2 - d0) / (d1 - d0) : 0.5f, 0.f), 0.99999994f);
+    const float wt = __ldg(&S.env_weight[(size_t)y * w + x]);
+    if (!(wt > 0.f) || !(S.env_total > 0.f)) return false;
+    const float theta = ((float)y + fy) / (float)h * NR_PI_F;
+    const float phi = (((float)x + fx) / (float)w - 0.5f) * 2.0f * NR_PI_F;
+    float st, ct, sp, cp;
+    sincosf(theta, &st, &ct);
+    sincosf(phi, &sp, &cp);
+    if (st < 1e-6f) return false;
+    dir = mk(st * cp, ct, st * sp);
+    pdf = wt / S.env_total * ((float)w * (float)h) / (2.0f * NR_PI_F * NR_PI_F * st);
+    return true;
+}
+// Density env_sample gives a direction (0 outside the sampled domain).
+__device__ __forceinline__ float env_pdf(const DeviceScene& S, f3 dir) {
+    const int4 info = __ldg(&S.tex_info[S.env_tex]);
+    const int w = info.x, h = info.y;
+    const float theta = acosf(fminf(fmaxf(dir.y, -1.f), 1.f));
+    const float fv = theta / NR_PI_F * (float)h;
+    const float fu = (atan2f(dir.z, dir.x) / 2.0f / NR_PI_F + 0.5f) * (float)w;
+    if (!(fv >= 0.f && fv < (float)h && fu >= 0.f && fu < (float)w)) return 0.f;
+    const int y = (int)fv, x = (int)fu;
+    const float st = sinf(theta);
+    if (st < 1e-6f || !(S.env_total > 0.f)) return 0.f;
+    return __ldg(&S.env_weight[(size_t)y * w + x]) / S.env_total * ((float)w * (float)h) /
+           (2.0f * NR_PI_F * NR_PI_F * st);
+}
+
 struct MatView {
     int type;
     f3 c0, c1;

@@ -52,6 +52,10 @@ struct DeviceScene {
     int32_t num_mats;
     int32_t env_tex;
     float env_gain;
+    const float* env_weight;   // environment sampling table (envis=1), see EnvTable in host_scene.h
+    const float* env_row_cdf;
+    const float* env_col_cdf;
+    float env_total;
     int32_t max_depth;        // deepest leaf (root = 0)
     int32_t num_nodes;        // internal nodes
 };
@@ -69,6 +73,7 @@ struct Policy {
                       // MIS, emitter hits dropped after a light sample, paths go on while u < prr
     int32_t coin;     // 1: a training coin is drawn after the jitter (RendererNRC::render)
     int32_t force_train;  // 1: every path is a training path (RendererNRC::render's first pass)
+    int32_t envis;    // 1: one environment light sample per light-sampling vertex, MIS against BSDF misses
     int32_t trav;     // traversal tests: 0 exact arithmetic only, 1 fast path with exact fallback (same hits)
 };
 
@@ -87,7 +92,8 @@ struct PathState {
     // shadow rays
     float4* sh_o;    // (origin, t limit)
     float4* sh_d;    // (direction, slot bits)
-    float4* sh_c;    // (contribution if unoccluded, unused)
+    float4* sh_c;    // (contribution if unoccluded, training record)
+    int32_t sh_cap;  // entries of the shadow-ray queue (1 or 2 per slot)
     // device counters (see Counter)
     uint32_t* counters;
 };

@@ -559,12 +559,92 @@ struct Cam {
 };
 
 // ---------------------------------------------------------------- scene
+// Environment sampling table of envis=1 (no counterpart in the reference):
+// the construction the library documents in host_scene.h (EnvTable),
+// restated. Cell (x, y) spans texels (x, y)..(x + 1, y + 1); weight = the
+// largest r + g + b of its corners (black past the edges) times
+// sin((y + 0.5) / h * 3.14159); cumulative sums in float, last entry 1.
+struct EnvTable {
+    int w = 0, h = 0;
+    std::vector<float> weight, row_cdf, col_cdf;
+    float total = 0.f;
+    void build(const Tex& t) {
+        w = t.w; h = t.h;
+        weight.assign((size_t)w * h, 0.f);
+        row_cdf.assign((size_t)h, 0.f);
+        col_cdf.assign((size_t)w * h, 0.f);
+        auto lum = [&](int x, int y) -> float {
+            if (x >= w || y >= h) return 0.f;
+            const V3& c = t.px[(size_t)y * w + x];
+            return c.x + c.y + c.z;
+        };
+        std::vector<float> rows((size_t)h, 0.f);
+        for (int y = 0; y < h; ++y) {
+            const float sn = std::sin(((float)y + 0.5f) / (float)h * 3.14159f);
+            float acc = 0.f;
+            for (int x = 0; x < w; ++x) {
+                float m = std::max(std::max(lum(x, y), lum(x + 1, y)), std::max(lum(x, y + 1), lum(x + 1, y + 1)));
+                float wt = m > 0.f ? m * sn : 0.f;
+                weight[(size_t)y * w + x] = wt;
+                acc += wt;
+                col_cdf[(size_t)y * w + x] = acc;
+            }
+            rows[y] = acc;
+            for (int x = 0; x < w; ++x) {
+                float& c = col_cdf[(size_t)y * w + x];
+                c = acc > 0.f ? c / acc : (float)(x + 1) / (float)w;
+            }
+            col_cdf[(size_t)y * w + w - 1] = 1.f;
+        }
+        float acc = 0.f;
+        for (int y = 0; y < h; ++y) { acc += rows[y]; row_cdf[y] = acc; }
+        total = acc;
+        for (int y = 0; y < h; ++y) row_cdf[y] = acc > 0.f ? row_cdf[y] / acc : (float)(y + 1) / (float)h;
+        row_cdf[h - 1] = 1.f;
+    }
+    static int upper(const float* c, int n, float r) {
+        int i = (int)(std::upper_bound(c, c + n, r) - c);
+        return i < n ? i : n - 1;
+    }
+    // a cell by its row and column CDFs, a uniform point in it, the direction
+    // the lookup maps it from, and the solid-angle density
+    bool sample(float r1, float r2, V3& dir, float& pdf) const {
+        const int y = upper(row_cdf.data(), h, r1);
+        const float c0 = y ? row_cdf[y - 1] : 0.f, c1 = row_cdf[y];
+        const float fy = std::min(std::max(c1 > c0 ? (r1 - c0) / (c1 - c0) : 0.5f, 0.f), 0.99999994f);
+        const float* col = col_cdf.data() + (size_t)y * w;
+        const int x = upper(col, w, r2);
+        const float d0 = x ? col[x - 1] : 0.f, d1 = col[x];
+        const float fx = std::min(std::max(d1 > d0 ? (r2 - d0) / (d1 - d0) : 0.5f, 0.f), 0.99999994f);
+        const float wt = weight[(size_t)y * w + x];
+        if (!(wt > 0.f) || !(total > 0.f)) return false;
+        const float theta = ((float)y + fy) / (float)h * 3.14159f;
+        const float phi = (((float)x + fx) / (float)w - 0.5f) * 2.0f * 3.14159f;
+        const float st = std::sin(theta), ct = std::cos(theta), sp = std::sin(phi), cp = std::cos(phi);
+        if (st < 1e-6f) return false;
+        dir = V3(st * cp, ct, st * sp);
+        pdf = wt / total * ((float)w * (float)h) / (2.0f * 3.14159f * 3.14159f * st);
+        return true;
+    }
+    float pdf_of(V3 d) const {
+        const float theta = std::acos(std::min(std::max(d.y, -1.f), 1.f));
+        const float fv = theta / 3.14159f * (float)h;
+        const float fu = (std::atan2(d.z, d.x) / 2.0f / 3.14159f + 0.5f) * (float)w;
+        if (!(fv >= 0.f && fv < (float)h && fu >= 0.f && fu < (float)w)) return 0.f;
+        const int y = (int)fv, x = (int)fu;
+        const float st = std::sin(theta);
+        if (st < 1e-6f || !(total > 0.f)) return 0.f;
+        return weight[(size_t)y * w + x] / total * ((float)w * (float)h) / (2.0f * 3.14159f * 3.14159f * st);
+    }
+};
+
 struct Scene {
     std::vector<Tri> tris;
     std::vector<Mat> mats;
     std::vector<Tex> texs;
     int env = -1;
     float env_gain = 1.0f;
+    EnvTable env_table;
     BVH bvh;
     Lights lights;
 };
@@ -580,12 +660,16 @@ struct Policy {
     // without MIS, an emitter hit counts only when the previous vertex took
     // no light sample, and a path continues while u < prr
     bool excl = false;
+    // envis=1 (no counterpart in the reference): one environment light sample
+    // more per light-sampling vertex, balance-heuristic MIS against BSDF misses
+    bool envis = false;
 };
 
 struct Counters { uint64_t rays = 0, shadow = 0, verts = 0; };
 
 // RendererPTLS::trace (src/renderer/rendererptls.cpp:13-94), recursive as there.
-V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float light_fac, int depth, Counters& C) {
+V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float light_fac, int depth, Counters& C,
+         float env_pb = 0.f) {
     C.rays++;
     BVH::Hit hit = S.bvh.intersect(orig, dir);
     if (hit.tri < 0) {
@@ -600,7 +684,9 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
         }
         float v = (float)(1 - std::acos((double)dir.y) / PI_D);
         float u = (float)(std::atan2((double)dir.z, (double)dir.x) / 2 / PI_D + 0.5);
-        return S.texs[S.env].uv(u, v) * S.env_gain;
+        V3 e = S.texs[S.env].uv(u, v) * S.env_gain;
+        if (env_pb > 0.f && S.env_table.w) e = e * (env_pb / (env_pb + S.env_table.pdf_of(dir)));
+        return e;
     }
     const Tri& T = S.tris[hit.tri];
     const Mat& M = S.mats[T.mat];
@@ -643,6 +729,28 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
             }
         }
     }
+    bool env_sampled = false;
+    if (P.envis && P.nee && mat_nee(M) && S.env >= 0 && S.env_table.w) {
+        env_sampled = true;
+        const float r1 = smp.random(), r2 = smp.random();
+        V3 we;
+        float pe;
+        if (S.env_table.sample(r1, r2, we, pe)) {
+            const float cosn = dot(normal, we);
+            if (cosn > 0.f) {
+                const bool last = P.maxdepth > 0 && depth + 1 >= P.maxdepth;
+                const float pb = last ? 0.f : mat_pdf(M, wo, normal, we);
+                C.shadow++;
+                BVH::Hit sh = S.bvh.intersect(hit_pos + we * 1e-3f, we);
+                if (sh.tri < 0) {
+                    float v = (float)(1 - std::acos((double)we.y) / PI_D);
+                    float u = (float)(std::atan2((double)we.z, (double)we.x) / 2 / PI_D + 0.5);
+                    V3 L = S.texs[S.env].uv(u, v) * S.env_gain;
+                    result = result + mat_bxdf(M, wo, normal, we, uv) * L * (cosn / (pe + pb));
+                }
+            }
+        }
+    }
     if (P.maxdepth > 0 && depth + 1 >= P.maxdepth) return result;
     // Russian roulette (src/renderer/rendererptls.cpp:80-83)
     float prr = depth < P.rrdepth ? 1.0f : P.prr;
@@ -651,7 +759,7 @@ V3 trace(const Scene& S, const Policy& P, Sampler& smp, V3 orig, V3 dir, float l
     V3 wi = mat_sample(M, smp, wo, normal);
     float pdf = mat_pdf(M, wo, normal, wi);
     V3 brdf = mat_bxdf(M, wo, normal, wi, uv);
-    V3 Li = trace(S, P, smp, hit_pos + wi * 1e-3f, wi, fac, depth + 1, C);
+    V3 Li = trace(S, P, smp, hit_pos + wi * 1e-3f, wi, fac, depth + 1, C, env_sampled ? pdf : 0.f);
     V3 contri = Li * std::fabs(dot(wi, normal)) * brdf / pdf / prr;
     return result + contri;
 }
@@ -712,6 +820,7 @@ void* port_scene_create(int ntri, const float* pos, const float* uv, const float
         T.pmax = vmax(T.p[0], vmax(T.p[1], T.p[2]));
     }
     S->env = env_tex; S->env_gain = env_gain;
+    if (env_tex >= 0 && env_tex < ntex) S->env_table.build(S->texs[env_tex]);
     S->lights.build(S->tris, S->mats);
     S->bvh.build(S->tris);
     return S;
@@ -780,6 +889,7 @@ void port_render_samples(void* s, const char* params, int npix, const int* pix_x
         P.excl = it != c.mp.end() && it->second == "nrc";
         coin = P.excl;
     }
+    P.envis = c.i("envis", 0) != 0;
     int w = c.i("imgw", 1), h = c.i("imgh", 1);
     int nth = threads < 1 ? 1 : threads;
     std::vector<Counters> C(nth);

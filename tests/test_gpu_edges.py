@@ -1,0 +1,93 @@
+"""Edge cases of the path against the oracle restatement (tolerances as in
+test_gpu_parity.py): an empty scene, a scene without lights, a one-pixel
+image, odd wavefront batch sizes, sample indices near 2^31, degenerate
+(zero-area) triangles, and rays along the coordinate axes, where the
+reference's slab test divides by d + 1e-9 (src/hierarchy/bvhnode.cpp:41)."""
+import numpy as np
+import pytest
+
+from oracle.bind import Oracle, pixel_grid
+from nuray_gb300 import scenes
+from test_gpu_parity import _sample_match, cornell_scene, gpu_scene
+
+pytestmark = pytest.mark.gpu
+
+CORNELL = "renderer=ptnee imgw=64 imgh=48 spp=4 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
+
+
+def test_empty_scene_renders_black_or_the_environment(gpu_lib):
+    from nuray_gb300 import Scene
+    S = Scene.from_arrays(np.zeros((0, 9), np.float32), np.zeros(0, np.int32), [dict(type=0, c0=[1, 1, 1])])
+    img = S.render(CORNELL)
+    assert img.shape == (48, 64, 3) and np.all(img == 0)
+    tri, t, _, _ = S.intersect(np.zeros((4, 3), np.float32), np.tile(np.float32([0, 0, 1]), (4, 1)))
+    assert np.all(tri == -1)
+    sky = np.full((8, 16, 3), 0.5, np.float32)
+    S.set_env(sky, 2.0)
+    img = S.render(CORNELL)
+    np.testing.assert_allclose(img, 1.0, rtol=1e-5)  # bilinear of a constant map (no edge texels reached)
+
+
+def test_scene_without_lights_matches_port(gpu_lib, port_lib):
+    sc = cornell_scene()
+    mats = [dict(m, type=0) if m["type"] == 5 else m for m in sc["mats"]]
+    sc = dict(sc, mats=mats)
+    S, P = gpu_scene(sc), Oracle("port", sc)
+    pix = pixel_grid(64, 48)[::7]
+    a = S.render_samples(CORNELL, pix, 4)
+    b = P.render_samples(CORNELL, pix, 4)
+    assert np.all(a == 0) and np.all(b == 0)  # no emitter, no environment
+
+
+def test_one_pixel_image_and_odd_waves(gpu_lib):
+    S = gpu_scene(cornell_scene())
+    one = S.render(CORNELL.replace("imgw=64 imgh=48", "imgw=1 imgh=1").replace("spp=4", "spp=257"))
+    assert one.shape == (1, 1, 3) and np.all(np.isfinite(one))
+    ref = S.render(CORNELL)
+    for wave in (777, 4097):
+        np.testing.assert_array_equal(S.render(CORNELL + f" wave={wave}"), ref)
+
+
+def test_sample_indices_near_2_31(gpu_lib, port_lib):
+    sc = cornell_scene()
+    S, P = gpu_scene(sc), Oracle("port", sc)
+    pix = pixel_grid(64, 48)[::11]
+    s0 = 2 ** 31 - 3
+    a = S.render_samples(CORNELL, pix, 2, sample0=s0)
+    b = P.render_samples(CORNELL, pix, 2, sample0=s0)
+    assert _sample_match(a, b) >= 0.97
+
+
+def test_degenerate_triangles_match_port(gpu_lib, port_lib):
+    sc = scenes.small_scene(7, env=False, textures=False)
+    pos = sc["pos"].copy()
+    rng = np.random.default_rng(3)
+    bad = rng.choice(pos.shape[0], 200, replace=False)
+    p = pos.reshape(-1, 3, 3)
+    p[bad[:100], 2] = p[bad[:100], 1]                       # two equal vertices
+    p[bad[100:], 2] = 0.5 * (p[bad[100:], 0] + p[bad[100:], 1])  # collinear
+    sc = dict(sc, pos=p.reshape(-1, 9).astype(np.float32))
+    S, P = gpu_scene(sc), Oracle("port", sc)
+    pix = pixel_grid(48, 32)
+    a = S.render_samples(sc["params"], pix, 4)
+    b = P.render_samples(sc["params"], pix, 4)
+    assert np.all(np.isfinite(a))
+    assert _sample_match(a, b) >= 0.97
+
+
+def test_axis_aligned_rays_match_port(gpu_lib, port_lib):
+    sc = scenes.small_scene(2, env=False, textures=False)
+    S, P = gpu_scene(sc), Oracle("port", sc)
+    rng = np.random.default_rng(8)
+    n = 6000
+    o = rng.uniform(-20, 20, (n, 3)).astype(np.float32)
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0.6, 0.8, 0], [0, -0.6, 0.8]], np.float32)
+    d = axes[rng.integers(0, len(axes), n)]
+    tri_g, t_g, _, _ = S.intersect(o, d)
+    tri_r, t_r, _, _ = P.intersect(o, d)
+    np.testing.assert_array_equal(tri_g >= 0, tri_r >= 0)
+    h = tri_r >= 0
+    assert h.mean() > 0.2
+    np.testing.assert_allclose(t_g[h], t_r[h], rtol=1e-5)
+    assert np.mean(tri_g[h] != tri_r[h]) < 1e-3
