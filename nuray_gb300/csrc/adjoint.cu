@@ -231,11 +231,12 @@ __device__ f3 replay(const AdjArgs& A, uint32_t key, uint32_t sample, int x, int
 
 // One thread per path: pass 1 for L, pass 2 for the gradient. Block-level
 // gradient histogram in shared memory, flushed with one atomic per entry.
-// 6 resident blocks per SM (80 registers, some spills): measured 56.7 Mpaths/s
-// on the 200k-triangle adjoint workload against 50.3 uncapped (123
-// registers) and 36.8 with the material code inlined.
+// 8 resident blocks per SM (64 registers, with spills): measured 62.7
+// Mpaths/s on the 200k-triangle adjoint workload, against 56.7 at 6 blocks,
+// 54.9 at 7, 50.8 at 4, 50.3 uncapped (123 registers) and 36.8 with the
+// material code inlined.
 #ifndef NR_ADJ_MINB
-#define NR_ADJ_MINB 6
+#define NR_ADJ_MINB 8
 #endif
 __global__ void __launch_bounds__(128, NR_ADJ_MINB) k_adjoint(AdjArgs A, const float* __restrict__ dldi, float* __restrict__ grad,
                                                  float* __restrict__ image_sum) {
