@@ -97,6 +97,9 @@ struct nr_nrc {
     float *y = nullptr, *out = nullptr, *loss = nullptr;
     float* xf = nullptr;  // FP32 staging of caller inputs
     float* loss_host = nullptr;  // pinned
+    bool tc = true;              // inference on tcgen05 (nrc_tc.cu); false: mma.sync (nrc.cu)
+    DevBuf errbuf;               // error word of the tensor-core inference
+    uint32_t* err_host = nullptr;  // pinned
 
     ~nr_nrc() {
         cudaSetDevice(device);
@@ -104,6 +107,8 @@ struct nr_nrc {
         pbuf.release();
         batch.release();
         if (loss_host) cudaFreeHost(loss_host);
+        if (err_host) cudaFreeHost(err_host);
+        errbuf.release();
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -595,8 +600,13 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             // launch reads them there, so the host never waits here.
             nr_nrc* c = s->nrc;
             const nr::NrcCtx& X = s->nrc_ctx;
-            nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)X.q_x, nr::nrc_rows_counted(&X.counters[0], cap, 0, 1),
-                                       s->nrc_pred, c->num_sms, st);
+            if (c->tc)
+                nr::nrc_launch_forward_tc(c->dev.wb_inf, c->dev.pinf, (const __nv_bfloat16*)X.q_x,
+                                          nr::nrc_rows_counted(&X.counters[0], cap, 0, 1), s->nrc_pred, c->num_sms,
+                                          s->ps.counters + nr::CNT_ERR, st);
+            else
+                nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)X.q_x,
+                                           nr::nrc_rows_counted(&X.counters[0], cap, 0, 1), s->nrc_pred, c->num_sms, st);
             nr::launch_nrc_apply(s->ps, X, s->nrc_pred, cap, st);
             nr::launch_nrc_targets(s->ps, X, c->y, 1e3f, st);
             NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
@@ -647,7 +657,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     S.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (c[nr::CNT_ERR] != 0)
         throw NrError(NR_ERR_DEVICE, "device error bits " + std::to_string(c[nr::CNT_ERR]) +
-                                         " (1 stack overflow, 2 step cap, 4 shadow queue full)");
+                                         " (1 stack overflow, 2 step cap, 4 shadow queue full, 8 tensor-core wait timed out)");
 }
 
 }  // namespace
@@ -999,7 +1009,12 @@ int nr_nrc_create(const char* params, nr_nrc** out) {
         n->eps = c.get_float("eps", 1e-8f);
         n->ema = c.get_float("ema", 0.99f);
         if (n->ema < 0.f || n->ema >= 1.f) throw NrError(NR_ERR_INVALID, "ema must be in [0, 1)");
+        n->tc = c.get_int("tc", 1) != 0;
         nr::nrc_setup();
+        nr::nrc_tc_setup();
+        n->errbuf.alloc(256);
+        NR_CUDA(cudaMemsetAsync(n->errbuf.p, 0, 4, n->stream));
+        NR_CUDA(cudaMallocHost(&n->err_host, 4));
         const size_t P = NRC_NUM_PARAMS;
         n->pbuf.alloc(6 * P * 4 + 2 * P * 2 + 512);
         float* f = n->pbuf.as<float>();
@@ -1081,10 +1096,16 @@ int nr_nrc_infer(nr_nrc* c, int32_t n, const float* x, float* out) {
         std::lock_guard<std::mutex> lk(c->mu);
         NR_CUDA(cudaSetDevice(c->device));
         nrc_upload_x(c, n, x);
-        nr::nrc_launch_forward(c->dev, c->x, nr::nrc_rows(n), c->out, nullptr, c->num_sms, c->stream);
+        if (c->tc)
+            nr::nrc_launch_forward_tc(c->dev.wb, c->dev.params, c->x, nr::nrc_rows(n), c->out, c->num_sms,
+                                      c->errbuf.as<uint32_t>(), c->stream);
+        else
+            nr::nrc_launch_forward(c->dev, c->x, nr::nrc_rows(n), c->out, nullptr, c->num_sms, c->stream);
         NR_CUDA(cudaMemcpyAsync(out, c->out, (size_t)n * 12, cudaMemcpyDeviceToHost, c->stream));
+        NR_CUDA(cudaMemcpyAsync(c->err_host, c->errbuf.p, 4, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaStreamSynchronize(c->stream));
         NR_CUDA(cudaGetLastError());
+        if (*c->err_host) throw NrError(NR_ERR_DEVICE, "tensor-core inference wait timed out");
     });
 }
 

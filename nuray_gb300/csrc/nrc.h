@@ -74,4 +74,11 @@ void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, const NrcRo
                             cudaStream_t st);
 void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t st);
 
+// The forward on the tcgen05 tensor cores (nrc_tc.cu) with the BF16 weights
+// wb and the FP32 biases of params (either copy of a cache): out [rows][3].
+// err (device word) gets bit 8 when a tensor-core wait timed out.
+void nrc_tc_setup();
+void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st);
+
 }  // namespace nr

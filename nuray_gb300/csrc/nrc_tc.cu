@@ -1,0 +1,268 @@
+// Cache inference on the 5th-generation tensor cores: the 80-64-64-64-64-3
+// MLP of nrc.cu as a chain of tcgen05.mma (kind::f16, BF16 operands, FP32
+// accumulators in tensor memory), 128 rows per CTA tile.
+//
+// Per tile: the 128 input rows go to shared memory in the canonical K-major
+// layout without swizzle (8-row x 16-byte core matrices; the leading byte
+// offset steps between core matrices along K, the stride byte offset between
+// 8-row groups); one thread issues the layer's MMAs (K = 16 each) and
+// commits them to an mbarrier; every thread then reads its row of the
+// 128 x N accumulator from tensor memory (tcgen05.ld 32x32b, warp w owns
+// lanes 32w..32w+31), adds the bias, applies ReLU, rounds to BF16 and writes
+// the row back to shared memory as the next layer's A operand. The weights
+// stay in shared memory for all tiles of the CTA. Every wait on the mbarrier
+// is bounded; a timeout sets an error bit, the CTA stops, frees its tensor
+// memory and returns.
+#include <cuda_bf16.h>
+
+#include "nrc.h"
+
+namespace nr {
+
+namespace {
+
+constexpr int IN = NRC_IN, H = NRC_H;
+constexpr int TM = 128;           // rows per tile (MMA M)
+constexpr int KC_IN = IN / 8;     // 16-byte chunks per input row (10)
+constexpr int KC_H = H / 8;       // 8
+// shared memory regions (bytes), each a multiple of 128
+constexpr int SM_W0 = 0;                              // 64 x 80
+constexpr int SM_W1 = SM_W0 + (H / 8) * KC_IN * 128;  // 64 x 64 each
+constexpr int SM_W2 = SM_W1 + (H / 8) * KC_H * 128;
+constexpr int SM_W3 = SM_W2 + (H / 8) * KC_H * 128;
+constexpr int SM_W4 = SM_W3 + (H / 8) * KC_H * 128;   // 16 x 64 (rows 3..15 zero)
+constexpr int SM_A = SM_W4 + 2 * KC_H * 128;          // 128 x 80 (hidden layers use 128 x 64)
+constexpr int SM_BIAS = SM_A + (TM / 8) * KC_IN * 128;
+constexpr int SM_BAR = SM_BIAS + (4 * H + 16) * 4;
+constexpr int SM_TOTAL = SM_BAR + 16;
+constexpr uint32_t TMEM_COLS = 64;
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory descriptor: start, leading and stride byte offsets
+// (all >> 4), the fixed 0b001 at bits 46-48, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor: FP32 D, BF16 A and B, both K-major, N, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+// Bounded wait for the mbarrier phase; false on timeout.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t phase) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's lane; the wait for the load
+// sits in the same statement, so no register is read before it lands.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// W [n][k] (row-major, k contiguous) into the canonical K-major layout.
+__device__ void load_w(unsigned char* sm, int off, const __nv_bfloat16* __restrict__ w, int rows, int rows_real, int k) {
+    const int kc = k / 8;
+    for (int i = threadIdx.x; i < rows * kc; i += blockDim.x) {
+        const int n = i / kc, c = i % kc;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (n < rows_real) v = *reinterpret_cast<const uint4*>(w + (size_t)n * k + 8 * c);
+        *reinterpret_cast<uint4*>(sm + off + (n / 8) * (kc * 128) + c * 128 + (n % 8) * 16) = v;
+    }
+}
+
+}  // namespace
+
+// Forward of the rows R over BF16 inputs [rows][80] with the BF16 weights
+// `wb` and the biases of `params`; out [rows][3] FP32. err bit 8 on a
+// tensor-core wait that timed out.
+__global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __restrict__ wb,
+                                                        const float* __restrict__ params,
+                                                        const __nv_bfloat16* __restrict__ x, NrcRows R,
+                                                        float* __restrict__ out, uint32_t* err) {
+    int m0, M;
+    if (!R.count) {
+        m0 = 0;
+        M = R.n;
+    } else {
+        const int total = min((int)*R.count, R.n);
+        const int chunk = (total + R.steps - 1) / R.steps;
+        m0 = R.step * chunk;
+        M = max(0, min(chunk, total - m0));
+    }
+    const int tiles = (M + TM - 1) / TM;
+    if ((int)blockIdx.x >= tiles) return;  // the whole CTA: no tensor memory taken
+    x += (size_t)m0 * IN;
+    out += (size_t)m0 * 3;
+
+    extern __shared__ __align__(1024) unsigned char sm[];
+    float* sbias = reinterpret_cast<float*>(sm + SM_BIAS);
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    load_w(sm, SM_W0, wb + NRC_OFF_W0, H, H, IN);
+    load_w(sm, SM_W1, wb + NRC_OFF_W1, H, H, H);
+    load_w(sm, SM_W2, wb + NRC_OFF_W2, H, H, H);
+    load_w(sm, SM_W3, wb + NRC_OFF_W3, H, H, H);
+    load_w(sm, SM_W4, wb + NRC_OFF_W4, 16, NRC_OUT_PAD, H);
+    for (int i = tid; i < 4 * H + 16; i += blockDim.x) {
+        const int offs[4] = {NRC_OFF_B0, NRC_OFF_B1, NRC_OFF_B2, NRC_OFF_B3};
+        sbias[i] = i < 4 * H ? params[offs[i / H] + i % H]
+                             : (i - 4 * H < NRC_OUT_PAD ? params[NRC_OFF_B4 + i - 4 * H] : 0.f);
+    }
+    const uint32_t bar = smem_u32(sm + SM_BAR);
+    if (tid == 0) {
+        s_abort = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_taddr)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = s_taddr;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0;
+
+    const uint32_t a_addr = smem_u32(sm + SM_A);
+    const uint32_t w_addr[5] = {smem_u32(sm + SM_W0), smem_u32(sm + SM_W1), smem_u32(sm + SM_W2), smem_u32(sm + SM_W3),
+                                smem_u32(sm + SM_W4)};
+
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        {  // input rows -> A (K = 80)
+            const int r = tid, row = tile * TM + r;
+            unsigned char* dst = sm + SM_A + (r / 8) * (KC_IN * 128) + (r % 8) * 16;
+#pragma unroll
+            for (int c = 0; c < KC_IN; ++c) {
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (row < M) v = *reinterpret_cast<const uint4*>(x + (size_t)row * IN + 8 * c);
+                *reinterpret_cast<uint4*>(dst + c * 128) = v;
+            }
+        }
+        for (int layer = 0; layer < 5; ++layer) {
+            const int k = layer == 0 ? IN : H;
+            const uint32_t sbo = (uint32_t)(k / 8) * 128u;
+            const uint32_t n = layer == 4 ? 16u : (uint32_t)H;
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after();
+#pragma unroll 1
+                for (int ks = 0; ks < k / 16; ++ks) {
+                    const uint64_t ad = sdesc(a_addr + (uint32_t)ks * 256u, 128u, sbo);
+                    const uint64_t bd = sdesc(w_addr[layer] + (uint32_t)ks * 256u, 128u, sbo);
+                    mma(tmem, ad, bd, idesc_bf16(n), ks > 0 ? 1u : 0u);
+                }
+                commit(bar);
+            }
+            const bool ok = wait_phase(bar, phase);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(err, 8u);
+                    s_abort = 1;
+                }
+                break;
+            }
+            fence_after();
+            const int r = tid, row = tile * TM + r;
+            if (layer < 4) {
+                unsigned char* dst = sm + SM_A + (r / 8) * (KC_H * 128) + (r % 8) * 16;
+                const float* b = sbias + layer * H;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float v[16];
+                    tmem_ld16(lane_base + (uint32_t)(16 * q), v);
+#pragma unroll
+                    for (int h2 = 0; h2 < 2; ++h2) {
+                        uint4 pk;
+                        const int c0 = 16 * q + 8 * h2;
+                        pk.x = pack_bf16(fmaxf(v[8 * h2 + 0] + b[c0 + 0], 0.f), fmaxf(v[8 * h2 + 1] + b[c0 + 1], 0.f));
+                        pk.y = pack_bf16(fmaxf(v[8 * h2 + 2] + b[c0 + 2], 0.f), fmaxf(v[8 * h2 + 3] + b[c0 + 3], 0.f));
+                        pk.z = pack_bf16(fmaxf(v[8 * h2 + 4] + b[c0 + 4], 0.f), fmaxf(v[8 * h2 + 5] + b[c0 + 5], 0.f));
+                        pk.w = pack_bf16(fmaxf(v[8 * h2 + 6] + b[c0 + 6], 0.f), fmaxf(v[8 * h2 + 7] + b[c0 + 7], 0.f));
+                        *reinterpret_cast<uint4*>(dst + (c0 / 8) * 128) = pk;
+                    }
+                }
+            } else {
+                float v[16];
+                tmem_ld16(lane_base, v);
+                if (row < M) {
+                    out[(size_t)row * 3 + 0] = v[0] + sbias[4 * H + 0];
+                    out[(size_t)row * 3 + 1] = v[1] + sbias[4 * H + 1];
+                    out[(size_t)row * 3 + 2] = v[2] + sbias[4 * H + 2];
+                }
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+size_t nrc_forward_tc_smem() { return (size_t)SM_TOTAL; }
+
+void nrc_tc_setup() {
+    cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc_forward_tc_smem());
+}
+
+void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st) {
+    const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
+    if (M <= 0) return;
+    int blocks = (M + TM - 1) / TM;
+    const int cap = num_sms * 3;  // three resident CTAs per SM by shared memory (64 tensor-memory columns each)
+    if (blocks > cap) blocks = cap;
+    k_nrc_forward_tc<<<blocks, 128, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, err);
+}
+
+}  // namespace nr
