@@ -267,7 +267,7 @@ def run_adjoint(args, local):
     paths1 = max(1, cnt["paths"])
     b_path = ((32 * cnt["nodes_visited"] + 36 * cnt["tris_tested"] + 32 * cnt["shadow_nodes_visited"]
                + 36 * cnt["shadow_tris_tested"]) / paths1 + 240 * cnt["rays"] / paths1 + 12)
-    achieved = 2 * b_path * paths / (ms / 1e3) / 1e9  # every path is traced twice
+    achieved = 2 * b_path * paths / (ms / 1e3) / 1e9  # every path is traced twice (wavefront pass + replay)
     out = {"metric": "Mpaths/s adjoint", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 2),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -275,7 +275,7 @@ def run_adjoint(args, local):
            "config": {"workload": f"path-replay adjoint, {sc['pos'].shape[0]} triangles, {len(sc['mats'])} "
                                   f"materials, {w}x{h}, spp={spp}, maxdepth 4, RR from depth 3",
                       "paths_per_step": w * h * spp},
-           "roofline": {"kernel": "k_adjoint (primal + adjoint replay)", "bound": "hbm",
+           "roofline": {"kernel": "wavefront pass + k_adjoint replay", "bound": "hbm",
                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(achieved / peak, 3), "peak_source": pk_kind, "traffic": None,
                         "bytes_per_path": round(2 * b_path, 1)},

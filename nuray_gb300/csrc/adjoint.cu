@@ -229,8 +229,10 @@ __device__ f3 replay(const AdjArgs& A, uint32_t key, uint32_t sample, int x, int
 
 }  // namespace
 
-// One thread per path: pass 1 for L, pass 2 for the gradient. Block-level
-// gradient histogram in shared memory, flushed with one atomic per entry.
+// One thread per path: the adjoint replay, given each path's radiance L
+// from the wavefront renderer (Lbuf[(pixel * spp + sample) * 3], max(0, L)
+// per channel). Block-level gradient histogram in shared memory, flushed
+// with one atomic per entry.
 // 8 resident blocks per SM (64 registers, with spills): measured 62.7
 // Mpaths/s on the 200k-triangle adjoint workload, against 56.7 at 6 blocks,
 // 54.9 at 7, 50.8 at 4, 50.3 uncapped (123 registers) and 36.8 with the
@@ -239,7 +241,7 @@ __device__ f3 replay(const AdjArgs& A, uint32_t key, uint32_t sample, int x, int
 #define NR_ADJ_MINB 8
 #endif
 __global__ void __launch_bounds__(128, NR_ADJ_MINB) k_adjoint(AdjArgs A, const float* __restrict__ dldi, float* __restrict__ grad,
-                                                 float* __restrict__ image_sum) {
+                                                 const float* __restrict__ Lbuf) {
     extern __shared__ float sg[];
     const int NG = A.S.num_mats * 7;
     for (int i = threadIdx.x; i < NG; i += blockDim.x) sg[i] = 0.f;
@@ -253,12 +255,8 @@ __global__ void __launch_bounds__(128, NR_ADJ_MINB) k_adjoint(AdjArgs A, const f
         int x = (int)(pidx % (uint32_t)A.pol.imgw), y = (int)(pidx / (uint32_t)A.pol.imgw);
         uint32_t key = (uint32_t)y * (uint32_t)A.pol.imgw + (uint32_t)x;
         uint32_t sample = A.sample0 + srel;
-        f3 L = replay<false>(A, key, sample, x, y, mk(0.f), mk(0.f), acc);
-        if (image_sum) {
-            atomicAdd(&image_sum[3 * pidx], smax(0.f, L.x));
-            atomicAdd(&image_sum[3 * pidx + 1], smax(0.f, L.y));
-            atomicAdd(&image_sum[3 * pidx + 2], smax(0.f, L.z));
-        }
+        const float* l = Lbuf + ((uint64_t)pidx * (uint64_t)A.spp + srel) * 3;
+        const f3 L = mk(l[0], l[1], l[2]);
         f3 delta = mk(L.x > 0.f ? dldi[3 * pidx] * inv_spp : 0.f, L.y > 0.f ? dldi[3 * pidx + 1] * inv_spp : 0.f,
                       L.z > 0.f ? dldi[3 * pidx + 2] * inv_spp : 0.f);
         if (delta.x == 0.f && delta.y == 0.f && delta.z == 0.f) continue;
@@ -269,16 +267,32 @@ __global__ void __launch_bounds__(128, NR_ADJ_MINB) k_adjoint(AdjArgs A, const f
         if (sg[i] != 0.f) atomicAdd(&grad[i], sg[i]);
 }
 
+// image_sum[pixel] = sum over its samples of max(0, L), in sample order.
+__global__ void k_image_from_L(const float* __restrict__ Lbuf, int npix, int spp, float* __restrict__ image_sum) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    float a = 0.f, b = 0.f, c = 0.f;
+    for (int s = 0; s < spp; ++s) {
+        const float* l = Lbuf + ((size_t)p * spp + s) * 3;
+        a += l[0]; b += l[1]; c += l[2];
+    }
+    image_sum[3 * p] = a; image_sum[3 * p + 1] = b; image_sum[3 * p + 2] = c;
+}
+
 void adjoint_setup() { cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); }
 
-void launch_adjoint(const AdjArgs& A, const float* dldi, float* grad, float* image_sum, int num_sms, cudaStream_t st) {
+void launch_image_from_L(const float* Lbuf, int npix, int spp, float* image_sum, cudaStream_t st) {
+    k_image_from_L<<<(npix + 255) / 256, 256, 0, st>>>(Lbuf, npix, spp, image_sum);
+}
+
+void launch_adjoint(const AdjArgs& A, const float* dldi, float* grad, const float* Lbuf, int num_sms, cudaStream_t st) {
     const uint64_t total = (uint64_t)A.npix * (uint64_t)A.spp;
     uint64_t blocks = (total + 127) / 128;
     uint64_t cap = (uint64_t)num_sms * 16;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     size_t smem = (size_t)A.S.num_mats * 7 * sizeof(float);
-    k_adjoint<<<(unsigned)blocks, 128, smem, st>>>(A, dldi, grad, image_sum);
+    k_adjoint<<<(unsigned)blocks, 128, smem, st>>>(A, dldi, grad, Lbuf);
 }
 
 }  // namespace nr

@@ -15,8 +15,11 @@ struct AdjArgs {
 };
 
 // grad: num_mats * 7 floats (albedo rgb, roughness, emission rgb), added to.
-// image_sum (may be null): per-pixel sum over samples of max(0, L).
+// Lbuf: each path's max(0, L) at [(pixel * spp + sample) * 3] (pixel =
+// y * imgw + x), as the wavefront renderer collects it.
 void adjoint_setup();
-void launch_adjoint(const AdjArgs& A, const float* dldi, float* grad, float* image_sum, int num_sms, cudaStream_t st);
+void launch_adjoint(const AdjArgs& A, const float* dldi, float* grad, const float* Lbuf, int num_sms, cudaStream_t st);
+// image_sum: per-pixel sum over samples of Lbuf.
+void launch_image_from_L(const float* Lbuf, int npix, int spp, float* image_sum, cudaStream_t st);
 
 }  // namespace nr

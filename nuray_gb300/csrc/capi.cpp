@@ -122,6 +122,7 @@ struct nr_scene {
     nr::Bvh bvh;
     nr::DeviceScene dev{};
     DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_mat;
+    DevBuf adj_L;  // per-path radiance for the adjoint replay
     DevBuf env_weight, env_row_cdf, env_col_cdf;  // environment sampling table (envis=1)
     int num_gpu_nodes = 0;
     // wavefront state
@@ -794,7 +795,16 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
             attr = true;
         }
         auto t0 = std::chrono::steady_clock::now();
-        nr::launch_adjoint(J, d_dldi, d_grad, image ? d_img : nullptr, s->num_sms, st);
+        // pass 1: every path's radiance from the wavefront renderer (scanline
+        // pixel order, so the buffer index is y * imgw + x)
+        s->adj_L.ensure((size_t)npix * A.spp * 12);
+        RenderArgs P1 = A;
+        P1.tile = false;
+        run_waves(s, P1, npix, nullptr, A.sample0, nullptr, s->adj_L.as<float>(), nullptr, nullptr, nullptr);
+        const uint64_t pass1_launches = s->stats.kernel_launches;
+        // pass 2: the adjoint replay of every path
+        nr::launch_adjoint(J, d_dldi, d_grad, s->adj_L.as<float>(), s->num_sms, st);
+        if (image) nr::launch_image_from_L(s->adj_L.as<float>(), npix, A.spp, d_img, st);
         NR_CUDA(cudaGetLastError());
         NR_CUDA(cudaMemcpyAsync(grad, d_grad, b_grad, cudaMemcpyDeviceToHost, st));
         if (image) NR_CUDA(cudaMemcpyAsync(image, d_img, b_img, cudaMemcpyDeviceToHost, st));
@@ -802,7 +812,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         if (image) for (size_t i = 0; i < (size_t)npix * 3; ++i) image[i] /= (float)A.spp;
         s->stats = nr_stats{};
         s->stats.paths = (uint64_t)npix * A.spp;
-        s->stats.kernel_launches = 1;  // k_adjoint
+        s->stats.kernel_launches = pass1_launches + 1 + (image ? 1 : 0);  // wavefront pass + k_adjoint (+ image)
         s->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }
