@@ -233,9 +233,11 @@ def run_reference(args, rank, world):
 
 
 def run_adjoint(args, local):
-    """--workload c5: each step is one nr_adjoint call (primal replay, then
-    adjoint replay of every path) for a fixed seeded d loss / d image; the
-    per-material gradient comes back to the host inside the timed region."""
+    """--workload c5: each step is one nr_adjoint call (a render pass that
+    records every bounce's hits and light-sample visibility, then the adjoint
+    replay of every path from those records) for a fixed seeded d loss / d
+    image; the per-material gradient comes back to the host inside the timed
+    region."""
     import torch
     from nuray_gb300 import Scene, build, inverse
     build.build()
@@ -267,7 +269,12 @@ def run_adjoint(args, local):
     paths1 = max(1, cnt["paths"])
     b_path = ((32 * cnt["nodes_visited"] + 36 * cnt["tris_tested"] + 32 * cnt["shadow_nodes_visited"]
                + 36 * cnt["shadow_tris_tested"]) / paths1 + 240 * cnt["rays"] / paths1 + 12)
-    achieved = 2 * b_path * paths / (ms / 1e3) / 1e9  # every path is traced twice (wavefront pass + replay)
+    # render pass: traversal and shading as in the ptnee frame, plus the hit
+    # record and visibility byte written per ray; replay: per ray the record
+    # read again, the shading reads (240 B) and the adjoint slot state (64 B)
+    rays_pp = cnt["rays"] / paths1
+    b_adj = b_path + rays_pp * (17 + 17 + 240 + 64) + 12
+    achieved = b_adj * paths / (ms / 1e3) / 1e9
     out = {"metric": "Mpaths/s adjoint", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 2),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -275,10 +282,12 @@ def run_adjoint(args, local):
            "config": {"workload": f"path-replay adjoint, {sc['pos'].shape[0]} triangles, {len(sc['mats'])} "
                                   f"materials, {w}x{h}, spp={spp}, maxdepth 4, RR from depth 3",
                       "paths_per_step": w * h * spp},
-           "roofline": {"kernel": "wavefront pass + k_adjoint replay", "bound": "hbm",
+           "roofline": {"kernel": "render pass with hit records + recorded replay", "bound": "hbm",
                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(achieved / peak, 3), "peak_source": pk_kind, "traffic": None,
-                        "bytes_per_path": round(2 * b_path, 1)},
+                        "bytes_per_path": round(b_adj, 1),
+                        "formula": "ptnee path bytes + rays x (17 record write + 17 read + 240 shading + 64 adjoint "
+                                   "state) + 12"},
            "gpu_launches": args.steps * S.stats()["kernel_launches"], "cpu_baseline": None, "e2e": None,
            "clocks": clk.summary()}
     print(json.dumps(out), flush=True)

@@ -329,8 +329,10 @@ int nr_scene_set_materials(nr_scene* scene, int32_t n, const nr_material* mats);
  * d image (W*H*3 floats, the image being the per-pixel mean of max(0, L)
  * that nr_render returns for the same params), writes d loss / d params
  * into dL_dparams: 7 floats per material (albedo r, g, b; roughness;
- * emission r, g, b). Each path is re-traced from its Philox key instead of
- * being stored. image (may be NULL) receives the primal image of the same
+ * emission r, g, b). Each wave of paths is rendered once, recording every
+ * bounce's hits and light-sample visibility, then replayed from its Philox
+ * keys and those records (params adj=mega: one thread per path, re-traced
+ * instead). image (may be NULL) receives the primal image of the same
  * samples. */
 int nr_adjoint(nr_scene* scene, const nr_camera* cam, const char* params, const float* dL_dimage, float* dL_dparams,
                float* image);

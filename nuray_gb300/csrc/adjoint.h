@@ -14,6 +14,28 @@ struct AdjArgs {
     int32_t spp;
 };
 
+// Per-slot state of the wavefront replay: each path's radiance and gradient
+// weight, its pending BSDF-factor terms (albedo terms and material in pk, w =
+// -1 for none; roughness terms and d fac / d alpha in pa), and per shadow ray
+// the light sample's gradient terms (sg0: albedo, roughness; sg1: emission,
+// w = material | light material << 16).
+struct AdjWave {
+    float4* L;
+    float4* delta;
+    float4* pk;
+    float4* pa;
+    float4* sg0;
+    float4* sg1;
+};
+void launch_adj_init(const PathState& P, const AdjWave& J, uint64_t base, int count, int npix, int spp,
+                     const float* Lbuf, const float* dldi, cudaStream_t st);
+// Shading of one bounce (after launch_trace or launch_sort_recorded), adding
+// to grad. vis: the bounce's light-sample visibility recorded by the first
+// pass, or null to trace the shadow rays here. Returns the kernels launched.
+int launch_adj_bounce_shading(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity,
+                              const AdjWave& J, const uint8_t* vis, float* grad, int num_sms, int shadow_blocks,
+                              cudaStream_t st);
+
 // grad: num_mats * 7 floats (albedo rgb, roughness, emission rgb), added to.
 // Lbuf: each path's max(0, L) at [(pixel * spp + sample) * 3] (pixel =
 // y * imgw + x), as the wavefront renderer collects it.

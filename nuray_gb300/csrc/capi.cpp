@@ -123,6 +123,7 @@ struct nr_scene {
     nr::DeviceScene dev{};
     DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_mat;
     DevBuf adj_L;  // per-path radiance for the adjoint replay
+    DevBuf adj_wave;  // per-slot state of the wavefront adjoint replay
     DevBuf env_weight, env_row_cdf, env_col_cdf;  // environment sampling table (envis=1)
     int num_gpu_nodes = 0;
     // wavefront state
@@ -359,6 +360,7 @@ void ensure_paths(nr_scene* s, int cap, int sh_mult = 1) {
     P.sh_d = (float4*)take(CS * f4);
     P.sh_c = (float4*)take(CS * f4);
     P.sh_cap = (int32_t)std::min<size_t>(CS, (size_t)INT32_MAX);
+    P.vis = nullptr;
     P.counters = (uint32_t*)take(nr::NUM_COUNTERS * 4);
     NR_CUDA(cudaMemsetAsync(P.counters, 0, nr::NUM_COUNTERS * 4, s->stream));
     s->capacity = cap;
@@ -418,6 +420,7 @@ struct RenderArgs {
     int nrc_direct;   // 1: light sample at the query vertex, cache for the rest
     int nrc_train_depth;  // > 0: training paths end in the cache from this depth on
     bool nrc_pre;         // renderer=nrc: one all-training pass before the samples (RendererNRC::render)
+    bool adj_mega;        // adjoint replay as one thread per path (adj=mega) instead of the wavefront
 };
 
 RenderArgs parse_args(const nr_camera* cam, const char* params) {
@@ -440,7 +443,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     // light sampling) or nrc (RendererNRC: light samples without MIS, the
     // cache asked from vertex path_lim on, path_lim_train on training paths)
     const std::string renderer = c.get_str("renderer");
-    a.pol.excl = a.pol.coin = a.pol.force_train = 0;
+    a.pol.excl = a.pol.coin = a.pol.force_train = a.pol.adj = 0;
     if (renderer.empty() || renderer == "ptnee") a.pol.nee = 1;
     else if (renderer == "pt") a.pol.nee = 0;
     else if (renderer == "nrc") { a.pol.nee = 1; a.pol.excl = 1; a.pol.coin = 1; }
@@ -455,6 +458,11 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.sample0 = c.get_int("sample0", 0);
     a.accumulate = c.get_int("accumulate", 0) != 0;
     a.tile = c.get_int("tile", 1) != 0;
+    {
+        const std::string adj = c.get_str("adj");
+        if (!adj.empty() && adj != "mega" && adj != "wave") throw NrError(NR_ERR_INVALID, "adj must be mega or wave");
+        a.adj_mega = adj == "mega";
+    }
     const bool nrc_mode = a.pol.excl != 0;
     a.nrc = c.get_int("nrc", nrc_mode ? 1 : 0) != 0;
     a.nrc_pre = nrc_mode && c.get_int("nrc_pre", 1) != 0;
@@ -661,6 +669,113 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                                          " (1 stack overflow, 2 step cap, 4 shadow queue full, 8 tensor-core wait timed out)");
 }
 
+// Both passes of the adjoint on the wavefront, wave by wave. Pass 1 renders
+// the wave (pol.adj: light samples traced wherever their gradient can be
+// nonzero), recording every bounce's hits and light-sample visibility, and
+// writes each path's radiance to adj_L. Pass 2 generates the same paths
+// again, queues the ones with a nonzero gradient weight and replays them
+// from the records: k_sort_recorded buckets the recorded hits by material,
+// k_shade_adj shades them and adds the gradient terms. Bounces past the
+// recorded depth (unbounded paths, or a record that would not fit) are traced
+// again (k_trace, k_shadow_adj). Returns the kernel launches.
+uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* d_dldi, float* d_grad) {
+    const uint64_t total = (uint64_t)npix * (uint64_t)A.spp;
+    const int cap = (int)std::min<uint64_t>(total, (uint64_t)A.wave);
+    ensure_paths(s, cap, 1);
+    cudaStream_t st = s->stream;
+    // slots, and shadow rays per bounce (one per path at most), of this wave size
+    const size_t C = (size_t)std::max(cap, 1), CS = C;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    // recorded bounces: maxdepth, or 16 without one; at most 32 GiB of records
+    int depth_rec = A.pol.maxdepth > 0 ? A.pol.maxdepth : 16;
+    const size_t per_bounce = al(C * 16) + al(C);
+    depth_rec = (int)std::max<size_t>(1, std::min<size_t>((size_t)depth_rec, (size_t(32) << 30) / per_bounce));
+    s->adj_wave.ensure(al(C * 16) * 4 + al(CS * 16) * 2 + per_bounce * (size_t)depth_rec);
+    char* p = s->adj_wave.as<char>();
+    auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
+    nr::AdjWave J;
+    J.L = (float4*)take(C * 16);
+    J.delta = (float4*)take(C * 16);
+    J.pk = (float4*)take(C * 16);
+    J.pa = (float4*)take(C * 16);
+    J.sg0 = (float4*)take(CS * 16);
+    J.sg1 = (float4*)take(CS * 16);
+    float4* rec_hit = (float4*)take(C * 16 * (size_t)depth_rec);
+    uint8_t* rec_vis = (uint8_t*)take(C * (size_t)depth_rec);
+    const float film_h = nr::film_height(A.cam);
+    nr::Policy pol1 = A.pol;
+    pol1.adj = 1;
+    uint64_t launches = 0;
+    NR_CUDA(cudaMemsetAsync(s->ps.counters, 0, nr::NUM_COUNTERS * 4, st));
+    auto live_after = [&](int bounce, int& live) {
+        // as in run_waves: the live count is read back once a wave may end early
+        if (A.pol.maxdepth == 0 || bounce >= 4) {
+            NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters, nr::NUM_COUNTERS * 4, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+            live = (int)s->counters_host[nr::CNT_IN];
+        }
+        return live > 0;
+    };
+    for (uint64_t base = 0; base < total; base += (uint64_t)cap) {
+        nr::WaveDesc W;
+        W.base = base;
+        W.count = (int)std::min<uint64_t>((uint64_t)cap, total - base);
+        W.npix = npix;
+        W.sample0 = (uint32_t)A.sample0;
+        W.pix_xy = nullptr;
+        W.tiled = 0;
+        // pass 1
+        nr::PathState P = s->ps;
+        nr::launch_reset_counters(P.counters, st);
+        nr::launch_raygen(P, W, A.cam, film_h, pol1, st);
+        launches += 2;
+        int live = W.count;
+        for (int bounce = 0;; ++bounce) {
+            if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
+            const bool rec = bounce < depth_rec;
+            P.hit = rec ? rec_hit + (size_t)bounce * C : s->ps.hit;
+            P.vis = rec ? rec_vis + (size_t)bounce * C : nullptr;
+            nr::launch_bounce(P, s->dev, pol1, cap, live, st, nullptr, false, nullptr);
+            std::swap(P.queue_in, P.queue_out);
+            launches += 4;
+            if (!live_after(bounce, live)) break;
+        }
+        nr::launch_collect(s->ps, W, s->adj_L.as<float>(), A.spp, st);
+        // pass 2
+        P = s->ps;
+        nr::launch_reset_counters(P.counters, st);
+        nr::launch_raygen(P, W, A.cam, film_h, A.pol, st);
+        nr::launch_adj_init(P, J, base, W.count, npix, A.spp, s->adj_L.as<float>(), d_dldi, st);
+        launches += 5;
+        live = W.count;
+        for (int bounce = 0;; ++bounce) {
+            if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
+            const bool rec = bounce < depth_rec;
+            const uint8_t* vis = nullptr;
+            if (rec) {
+                P.hit = rec_hit + (size_t)bounce * C;
+                vis = rec_vis + (size_t)bounce * C;
+                nr::launch_sort_recorded(P, s->dev, cap, st);
+            } else {
+                P.hit = s->ps.hit;
+                nr::launch_trace(P, s->dev, A.pol, cap, st);
+            }
+            launches += 2 + nr::launch_adj_bounce_shading(P, s->dev, A.pol, cap, J, vis, d_grad, s->num_sms,
+                                                          nr::shadow_grid(), st);
+            nr::launch_advance(P.counters, st);
+            std::swap(P.queue_in, P.queue_out);
+            if (!live_after(bounce, live)) break;
+        }
+    }
+    NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters, nr::NUM_COUNTERS * 4, cudaMemcpyDeviceToHost, st));
+    NR_CUDA(cudaStreamSynchronize(st));
+    NR_CUDA(cudaGetLastError());
+    if (s->counters_host[nr::CNT_ERR] != 0)
+        throw NrError(NR_ERR_DEVICE, "device error bits " + std::to_string(s->counters_host[nr::CNT_ERR]) +
+                                         " in the adjoint (1 stack overflow, 2 step cap, 4 shadow queue full)");
+    return launches;
+}
+
 }  // namespace
 
 extern "C" {
@@ -795,15 +910,19 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
             attr = true;
         }
         auto t0 = std::chrono::steady_clock::now();
-        // pass 1: every path's radiance from the wavefront renderer (scanline
-        // pixel order, so the buffer index is y * imgw + x)
+        // every path's radiance (scanline pixel order, so the buffer index is
+        // (y * imgw + x) * spp + sample), then the replay of every path
         s->adj_L.ensure((size_t)npix * A.spp * 12);
-        RenderArgs P1 = A;
-        P1.tile = false;
-        run_waves(s, P1, npix, nullptr, A.sample0, nullptr, s->adj_L.as<float>(), nullptr, nullptr, nullptr);
-        const uint64_t pass1_launches = s->stats.kernel_launches;
-        // pass 2: the adjoint replay of every path
-        nr::launch_adjoint(J, d_dldi, d_grad, s->adj_L.as<float>(), s->num_sms, st);
+        uint64_t launches = 0;
+        if (A.adj_mega) {
+            RenderArgs P1 = A;
+            P1.tile = false;
+            run_waves(s, P1, npix, nullptr, A.sample0, nullptr, s->adj_L.as<float>(), nullptr, nullptr, nullptr);
+            nr::launch_adjoint(J, d_dldi, d_grad, s->adj_L.as<float>(), s->num_sms, st);
+            launches = s->stats.kernel_launches + 1;
+        } else {
+            launches = adjoint_waves(s, A, npix, d_dldi, d_grad);
+        }
         if (image) nr::launch_image_from_L(s->adj_L.as<float>(), npix, A.spp, d_img, st);
         NR_CUDA(cudaGetLastError());
         NR_CUDA(cudaMemcpyAsync(grad, d_grad, b_grad, cudaMemcpyDeviceToHost, st));
@@ -812,7 +931,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         if (image) for (size_t i = 0; i < (size_t)npix * 3; ++i) image[i] /= (float)A.spp;
         s->stats = nr_stats{};
         s->stats.paths = (uint64_t)npix * A.spp;
-        s->stats.kernel_launches = pass1_launches + 1 + (image ? 1 : 0);  // wavefront pass + k_adjoint (+ image)
+        s->stats.kernel_launches = launches + (image ? 1 : 0);
         s->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }

@@ -146,6 +146,20 @@ __global__ void __launch_bounds__(128, NR_TRACE_MINB) k_trace(PathState P, Devic
     }
 }
 
+// The sort of k_trace for hits recorded by an earlier pass over the same
+// paths (P.hit pointing at that bounce's record): no traversal.
+__global__ void k_sort_recorded(PathState P, DeviceScene S, int capacity) {
+    const uint32_t n = P.counters[CNT_IN];
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int slot = P.queue_in[idx];
+        const int tri = __float_as_int(P.hit[slot].w);
+        int cat = CAT_MISS;
+        if (tri >= 0) cat = S.mats[__float_as_int(__ldg(&S.tri_geo[3 * tri + 1]).w)].type;
+        const int pos = warp_append_keyed(cat, &P.counters[CNT_CAT]);
+        P.sorted[(size_t)cat * capacity + pos] = slot;
+    }
+}
+
 // Shadow rays, persistent like k_trace: occluded when any reachable triangle
 // has t <= the ray's limit (any_hit); unoccluded rays add their NEE term.
 template <bool COUNT, bool FAST>
@@ -161,7 +175,10 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
         uint32_t idx = base + lane;
         if (idx < n) {
             float4 o = P.sh_o[idx], d = P.sh_d[idx];
-            if (!any_hit<FAST>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr, COUNT ? &nt : nullptr)) {
+            const bool occluded =
+                any_hit<FAST>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr, COUNT ? &nt : nullptr);
+            if (P.vis) P.vis[__float_as_int(d.w)] = occluded ? 0 : 1;
+            if (!occluded) {
                 int slot = __float_as_int(d.w);
                 float4 c = P.sh_c[idx];
                 float4 r = P.rad[slot];
@@ -329,9 +346,10 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
         else fac = 1.0f - mis;
         f3 brdf = mat_bxdf(M, wo, normal, wl);
         f3 Ll = Ke / norm2(light_vec) * smax(0.f, cos_l) / light_pdf;
-        f3 c = Ll * brdf * smax(0.f, dot(normal, normalized(light_pos - hit_pos))) * mis;
+        const float geo = smax(0.f, dot(normal, normalized(light_pos - hit_pos)));
+        f3 c = Ll * brdf * geo * mis;
         c = c * T;
-        if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
+        if (c.x != 0.f || c.y != 0.f || c.z != 0.f || (pol.adj && cos_l > 0.f && geo > 0.f && mis > 0.f)) {
             // Visible iff the closest t satisfies t + 2e-3 > |light_vec| (in
             // double there), i.e. occluded iff some hit has t <= |lv| - 2e-3.
             double lim = (double)norm(light_vec) - 2e-3;
@@ -577,6 +595,13 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
     k_advance<<<1, 1, 0, st>>>(P.counters);
 }
 
+void launch_trace(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, cudaStream_t st) {
+    if (pol.trav) k_trace<false, true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
+    else k_trace<false, false><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity);
+}
+void launch_advance(uint32_t* counters, cudaStream_t st) { k_advance<<<1, 1, 0, st>>>(counters); }
+int shadow_grid() { return g_shadow_blocks; }
+
 void launch_reset_counters(uint32_t* counters, cudaStream_t st) { k_reset_counters<<<1, 32, 0, st>>>(counters); }
 
 // The counts live on the device: grid-stride loops over a grid sized for
@@ -585,6 +610,9 @@ static int count_grid(int cap) {
     int b = (cap + 255) / 256;
     const int most = 8 * g_num_sms;
     return b < 1 ? 1 : (b > most ? most : b);
+}
+void launch_sort_recorded(const PathState& P, const DeviceScene& S, int capacity, cudaStream_t st) {
+    k_sort_recorded<<<count_grid(capacity), 256, 0, st>>>(P, S, capacity);
 }
 void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int cap, cudaStream_t st) {
     k_nrc_apply<<<count_grid(cap), 256, 0, st>>>(P, C, pred);

@@ -25,6 +25,13 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
 void launch_nrc_apply(const PathState& P, const NrcCtx& C, const float* pred, int cap, cudaStream_t st);
 void launch_nrc_targets(const PathState& P, const NrcCtx& C, float* y, float clamp_max, cudaStream_t st);
 void launch_reset_counters(uint32_t* counters, cudaStream_t st);
+// The closest-hit + material-sort and advance steps alone, for wavefronts
+// that shade with kernels of their own (the adjoint replay).
+void launch_trace(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, cudaStream_t st);
+void launch_advance(uint32_t* counters, cudaStream_t st);
+// k_trace's sort by shading category for hits recorded in P.hit by an earlier pass
+void launch_sort_recorded(const PathState& P, const DeviceScene& S, int capacity, cudaStream_t st);
+int shadow_grid();  // blocks of the persistent shadow-ray kernels
 void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, cudaStream_t st);
 void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st);
 void launch_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8, cudaStream_t st);

@@ -75,6 +75,8 @@ struct Policy {
     int32_t force_train;  // 1: every path is a training path (RendererNRC::render's first pass)
     int32_t envis;    // 1: one environment light sample per light-sampling vertex, MIS against BSDF misses
     int32_t trav;     // traversal tests: 0 exact arithmetic only, 1 fast path with exact fallback (same hits)
+    int32_t adj;      // 1: a light sample is traced whenever its gradient can be nonzero, even where
+                      // its contribution is zero (the adjoint's first pass); radiance unchanged
 };
 
 // Wavefront path state, structure of arrays, one slot per in-flight path.
@@ -94,6 +96,7 @@ struct PathState {
     float4* sh_d;    // (direction, slot bits)
     float4* sh_c;    // (contribution if unoccluded, training record)
     int32_t sh_cap;  // entries of the shadow-ray queue (1 or 2 per slot)
+    uint8_t* vis;    // null, or per slot: 1 if its light sample of this bounce was unoccluded
     // device counters (see Counter)
     uint32_t* counters;
 };

@@ -122,3 +122,30 @@ def test_adjoint_image_equals_render_and_gradient_is_linear_in_dl(gpu_lib):
     np.testing.assert_allclose(img, ref, rtol=1e-3, atol=1e-4)
     g2 = S.adjoint(PARAMS, 2 * W)
     np.testing.assert_allclose(g2, 2 * g1, rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("case", ["box", "box_unbounded_small_waves", "textured_env"])
+def test_wavefront_replay_equals_one_thread_per_path(gpu_lib, case):
+    """The default replay runs on the wavefront (trace and sort, shade, shadow
+    rays per bounce); adj=mega replays each path in one thread. Same paths and
+    the same terms, summed in another order: equal to float rounding."""
+    from nuray_gb300 import scenes
+    if case == "textured_env":
+        sc = scenes.small_scene(4, env=True, textures=True)
+        from test_gpu_parity import gpu_scene
+        S = gpu_scene(sc)
+        params = sc["params"].replace("spp=1 ", "spp=4 ") + " rrdepth=3 maxdepth=6"
+        w, h = (int(params.split(k)[1].split()[0]) for k in ("imgw=", "imgh="))
+    else:
+        sc = box_scene()
+        S = gpu(sc)
+        params = PARAMS
+        if case == "box_unbounded_small_waves":
+            params = PARAMS.replace("rrdepth=2 maxdepth=5", "rrdepth=3 maxdepth=0") + " wave=5000"
+        w, h = 40, 30
+    W = loss_weights((h, w, 3), 5)
+    gw, img_w = S.adjoint(params, W, want_image=True)
+    gm, img_m = S.adjoint(params + " adj=mega", W, want_image=True)
+    np.testing.assert_array_equal(img_w, img_m)
+    assert np.abs(gm).max() > 0
+    np.testing.assert_allclose(gw, gm, rtol=1e-3, atol=1e-5 * np.abs(gm).max())
