@@ -109,11 +109,22 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // extra warps pay: measured on GB300 for the 1M-triangle frame, 566
 // Mpaths/s at 10 against 530 with no cap (53 registers, 36 warps) and 541
 // at 12 (40 registers, with spills).
+// Loop shape (NR_WW bits): 1 closest hit while-while with postponed leaves
+// (closest_hit_ww), 8 the same without postponing; 2 / 4 any hit likewise;
+// 0 the if-if loops (closest_hit, any_hit). Measured for the 1M-triangle
+// frame: if-if 585.5 Mpaths/s; postponed leaves in both 591.9 (k_trace
+// -14 %, k_shadow slower: its first leaf often holds the occluder); in
+// closest hit only 636.6; with any hit while-while without postponing 645.4;
+// closest hit without postponing too 606.6. With this shape the caps stay
+// best at 10 / 10 (trace 8: 621.8, 12: 629.6; shadow 8: 639.9, 12: 603.1).
 #ifndef NR_TRACE_MINB
 #define NR_TRACE_MINB 10
 #endif
 #ifndef NR_SHADOW_MINB
 #define NR_SHADOW_MINB 10
+#endif
+#ifndef NR_WW
+#define NR_WW 5
 #endif
 
 template <bool COUNT, bool FAST>
@@ -131,8 +142,10 @@ __global__ void __launch_bounds__(128, NR_TRACE_MINB) k_trace(PathState P, Devic
             int slot = P.queue_in[idx];
             f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
             float t, b1, b2;
-            int tri = closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
-                                        COUNT ? &nt : nullptr);
+            int tri = (NR_WW & 9) ? closest_hit_ww<FAST, (NR_WW & 1) != 0>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                                   COUNT ? &nt : nullptr)
+                            : closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                                COUNT ? &nt : nullptr);
             P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
             int cat = CAT_MISS;
             if (tri >= 0) cat = S.mats[__float_as_int(__ldg(&S.tri_geo[3 * tri + 1]).w)].type;
@@ -176,7 +189,10 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
         if (idx < n) {
             float4 o = P.sh_o[idx], d = P.sh_d[idx];
             const bool occluded =
-                any_hit<FAST>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr, COUNT ? &nt : nullptr);
+                (NR_WW & 6) ? any_hit_ww<FAST, (NR_WW & 2) != 0>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                         COUNT ? &nt : nullptr)
+                      : any_hit<FAST>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                      COUNT ? &nt : nullptr);
             if (P.vis) P.vis[__float_as_int(d.w)] = occluded ? 0 : 1;
             if (!occluded) {
                 int slot = __float_as_int(d.w);

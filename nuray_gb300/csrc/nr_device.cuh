@@ -320,6 +320,179 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
 // Shadow query: true when some reachable triangle has a reference hit with
 // t <= tmax (the complement of `t + 2e-3 > |light_vec|` of
 // src/renderer/rendererptls.cpp:71 for the closest hit).
+// While-while traversal with postponed leaves (Aila and Laine, "Understanding
+// the efficiency of ray traversal on GPUs", HPG 2009): a lane that reaches a
+// leaf keeps it aside and goes on through inner nodes until every active lane
+// of its warp holds a leaf; then the warp tests leaves together. Same hits as
+// closest_hit: the winner is the minimum t, ties to the larger leaf start and
+// then the earlier triangle of the leaf, whatever the visiting order, and a
+// subtree is only skipped when its entry distance exceeds the pruning limit
+// of the best hit so far, which never undercuts the final one.
+// Refs: inner nodes >= 0, leaves < 0; NR_TRAV_END (no node) ends the walk.
+#define NR_TRAV_END 0x7fffffff
+
+template <bool FAST, bool SPEC = true>
+__device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, float& best_t, float& best_b1,
+                                              float& best_b2, uint32_t* err, uint32_t* nodes_visited = nullptr,
+                                              uint32_t* tris_tested = nullptr) {
+    best_t = 1e18f; best_b1 = 0.f; best_b2 = 0.f;
+    int best = -1, best_leaf = -1;
+    if (S.root_ref == INT32_MIN) return -1;
+    SlabRay R = make_slab_ray(o, d);
+    float te;
+    if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return -1;
+    int2 stack[NR_STACK];
+    int sp = 0;
+    int ref = S.root_ref;
+    int leaf = 0;  // postponed leaf (< 0), or none (>= 0)
+    uint32_t nv = 0, nt = 0;
+    int budget = 2 * S.num_nodes + 8;
+    // the next stacked subtree that can still hold a hit, or NR_TRAV_END
+    auto pop = [&]() {
+        while (sp > 0) {
+            --sp;
+            const int2 e = stack[sp];
+            if (__int_as_float(e.y) <= best_t * (1.0f + NR_PRUNE_MARGIN)) return e.x;
+        }
+        return (int)NR_TRAV_END;
+    };
+    while (ref != NR_TRAV_END) {
+        while ((unsigned)ref < (unsigned)NR_TRAV_END) {
+            if (--budget < 0) { atomicOr(err, 2u); ref = NR_TRAV_END; leaf = 0; break; }
+            const GpuNode& N = S.nodes[ref];
+            float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
+            int4 k = __ldg(&N.d);
+            ++nv;
+            float t0, t1;
+            bool h0 = FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
+            bool h1 = FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
+            const float lim = best_t * (1.0f + NR_PRUNE_MARGIN);
+            h0 = h0 && t0 <= lim;
+            h1 = h1 && t1 <= lim;
+            if (h0 && h1) {
+                int nr = k.x, fr = k.y;
+                float ft = t1;
+                if (t1 < t0) { nr = k.y; fr = k.x; ft = t0; }
+                if (sp >= NR_STACK) { atomicOr(err, 1u); ref = NR_TRAV_END; leaf = 0; break; }
+                stack[sp] = make_int2(fr, __float_as_int(ft)); ++sp;
+                ref = nr;
+            } else if (h0) {
+                ref = k.x;
+            } else if (h1) {
+                ref = k.y;
+            } else {
+                ref = pop();
+            }
+            if (SPEC) {
+                if (ref < 0 && leaf >= 0) {  // first leaf: keep it aside, go on
+                    leaf = ref;
+                    ref = pop();
+                }
+                if (!__any_sync(__activemask(), leaf >= 0)) break;
+            }
+        }
+        if (!SPEC && ref < 0) {
+            leaf = ref;
+            ref = pop();
+        }
+        while (leaf < 0) {
+            int first = leaf_first(leaf), cnt = leaf_count(leaf);
+            float lt = 1e18f;
+            int li = -1;
+            for (int i = 0; i < cnt; ++i) {
+                int ti = first + i;
+                float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
+                ++nt;
+                float t, u, v;
+                if (FAST ? tri_test_fast(o, d, g0, g1, g2, lt, t, u, v) : tri_test(o, d, g0, g1, g2, lt, t, u, v)) {
+                    lt = t; li = ti;
+                }
+            }
+            if (li >= 0 && (lt < best_t || (lt == best_t && first > best_leaf))) {
+                best_t = lt; best = li; best_leaf = first;
+            }
+            // a second leaf reached while this one waited goes next
+            leaf = ref;
+            if (ref < 0) ref = pop();
+        }
+    }
+    if (nodes_visited) *nodes_visited += nv;
+    if (tris_tested) *tris_tested += nt;
+    if (best >= 0) {
+        float4 g0 = __ldg(&S.tri_geo[3 * best]), g1 = __ldg(&S.tri_geo[3 * best + 1]), g2 = __ldg(&S.tri_geo[3 * best + 2]);
+        float t;
+        tri_test(o, d, g0, g1, g2, 3.0e38f, t, best_b1, best_b2);
+    }
+    return best;
+}
+
+// Any hit with t <= tmax, traversed as closest_hit_ww (SPEC), or while-while
+// without postponing: a lane's inner-node loop ends at its first leaf.
+template <bool FAST, bool SPEC>
+__device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, float tmax, uint32_t* err,
+                                           uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr) {
+    if (S.root_ref == INT32_MIN) return false;
+    SlabRay R = make_slab_ray(o, d);
+    float te;
+    if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return false;
+    const float lim = tmax * (1.0f + NR_PRUNE_MARGIN);
+    int stack[NR_STACK];
+    int sp = 0;
+    int ref = S.root_ref;
+    int leaf = 0;
+    const float limit = fminf(1e18f, __uint_as_float(__float_as_uint(tmax) + 1u));  // accepts t <= tmax
+    int budget = 2 * S.num_nodes + 8;
+    while (ref != NR_TRAV_END) {
+        while ((unsigned)ref < (unsigned)NR_TRAV_END) {
+            if (--budget < 0) { atomicOr(err, 2u); return false; }
+            const GpuNode& N = S.nodes[ref];
+            float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
+            int4 k = __ldg(&N.d);
+            if (nodes_visited) ++*nodes_visited;
+            float t0, t1;
+            bool h0 = (FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0)) && t0 <= lim;
+            bool h1 = (FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1)) && t1 <= lim;
+            if (h0 && h1) {
+                int nr = k.x, fr = k.y;
+                if (t1 < t0) { nr = k.y; fr = k.x; }
+                if (sp >= NR_STACK) { atomicOr(err, 1u); return false; }
+                stack[sp++] = fr;
+                ref = nr;
+            } else if (h0) {
+                ref = k.x;
+            } else if (h1) {
+                ref = k.y;
+            } else {
+                ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+            }
+            if (SPEC) {
+                if (ref < 0 && leaf >= 0) {
+                    leaf = ref;
+                    ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+                }
+                if (!__any_sync(__activemask(), leaf >= 0)) break;
+            }
+        }
+        if (!SPEC && ref < 0) {  // the leaf reached: tested at once
+            leaf = ref;
+            ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+        }
+        while (leaf < 0) {
+            int first = leaf_first(leaf), cnt = leaf_count(leaf);
+            for (int i = 0; i < cnt; ++i) {
+                int ti = first + i;
+                float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
+                if (tris_tested) ++*tris_tested;
+                float t, u, v;
+                if (FAST ? tri_test_fast(o, d, g0, g1, g2, limit, t, u, v) : tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
+            }
+            leaf = ref;
+            if (ref < 0) ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+        }
+    }
+    return false;
+}
+
 template <bool FAST = true>
 __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float tmax, uint32_t* err,
                                         uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr) {
