@@ -117,6 +117,8 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // closest hit only 636.6; with any hit while-while without postponing 645.4;
 // closest hit without postponing too 606.6. With this shape the caps stay
 // best at 10 / 10 (trace 8: 621.8, 12: 629.6; shadow 8: 639.9, 12: 603.1).
+// Also measured and dropped for the shadow rays: dynamic fetch of new rays
+// into idle lanes (Aila and Laine 2009) at 4, 8 or 16 idle lanes, 571.
 #ifndef NR_TRACE_MINB
 #define NR_TRACE_MINB 10
 #endif
