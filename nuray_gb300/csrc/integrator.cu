@@ -418,8 +418,15 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
 
 // Shades the bucketed queue: categories are contiguous, so each warp mostly
 // runs one material's code.
+// Shading asks for 8 resident 128-thread blocks per SM (64 registers, a
+// few spills) instead of the 5 its 94 registers allow: it waits on memory,
+// and the extra warps pay. 1M-triangle frame: 646.3 Mpaths/s uncapped,
+// 651.8 at 6, 657.4 at 8, 647.3 at 10, 629.7 at 12.
+#ifndef NR_SHADE_MINB
+#define NR_SHADE_MINB 8
+#endif
 template <bool NRC>
-__global__ void __launch_bounds__(128) k_shade(PathState P, DeviceScene S, Policy pol, int capacity, NrcCtx C) {
+__global__ void __launch_bounds__(128, NR_SHADE_MINB) k_shade(PathState P, DeviceScene S, Policy pol, int capacity, NrcCtx C) {
     uint32_t cnt[NUM_CAT], start[NUM_CAT];
     uint32_t total = 0;
 #pragma unroll
