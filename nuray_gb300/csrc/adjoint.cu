@@ -413,7 +413,13 @@ __global__ void k_adj_setin(uint32_t* counters) {
     counters[CNT_WORK] = 0;
 }
 
-__global__ void __launch_bounds__(128) k_shade_adj(PathState P, DeviceScene S, Policy pol, int capacity, AdjWave J,
+// 8 resident blocks per SM asked of the register allocator (64 registers,
+// some spills, against 128 registers and 4 blocks uncapped): C5 552.1
+// against 535.1 Mpaths/s on one box, 534.8 at 6.
+#ifndef NR_ADJ_SHADE_MINB
+#define NR_ADJ_SHADE_MINB 8
+#endif
+__global__ void __launch_bounds__(128, NR_ADJ_SHADE_MINB) k_shade_adj(PathState P, DeviceScene S, Policy pol, int capacity, AdjWave J,
                                                    const uint8_t* __restrict__ vis, float* __restrict__ grad) {
     extern __shared__ float sg[];
     const int NG = S.num_mats * 7;
