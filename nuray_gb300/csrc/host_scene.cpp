@@ -147,6 +147,20 @@ std::string read_image(const std::string& path, int& w, int& h, std::vector<floa
     {
         unsigned char sig[8] = {0};
         f.read(reinterpret_cast<char*>(sig), 8);
+        if (f.gcount() >= 3 && sig[0] == 0xFF && sig[1] == 0xD8 && sig[2] == 0xFF) {
+            f.seekg(0, std::ios::end);
+            std::vector<uint8_t> bytes((size_t)f.tellg());
+            f.seekg(0);
+            f.read(reinterpret_cast<char*>(bytes.data()), (std::streamsize)bytes.size());
+            if (!f) return "cannot read " + path;
+            std::vector<uint8_t> px;
+            std::string err = jpeg_decode(bytes, w, h, px);
+            if (!err.empty()) return err + ": " + path;
+            // the same 8-bit to linear mapping as for PNG below
+            rgb.resize(px.size());
+            for (size_t i = 0; i < px.size(); ++i) rgb[i] = (float)std::pow((double)(px[i] * 257) / 65535.0, (double)2.2f);
+            return "";
+        }
         if (f.gcount() == 8 && sig[0] == 0x89 && sig[1] == 'P' && sig[2] == 'N' && sig[3] == 'G') {
             f.seekg(0, std::ios::end);
             std::vector<uint8_t> bytes((size_t)f.tellg());
@@ -207,7 +221,7 @@ std::string read_image(const std::string& path, int& w, int& h, std::vector<floa
         for (size_t i = 0; i < raw.size(); ++i) rgb[i] = (float)std::pow(raw[i] / 255.0, (double)2.2f);
         return "";
     }
-    return "unsupported image format (PNG, PFM or binary PPM): " + path;
+    return "unsupported image format (PNG, JPEG, PFM or binary PPM): " + path;
 }
 
 void build_env_table(const float* rgb, int w, int h, EnvTable& T) {

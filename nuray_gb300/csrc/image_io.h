@@ -21,6 +21,11 @@ namespace nr {
 // an error message.
 std::string png_decode(const std::vector<uint8_t>& file, int& width, int& height, std::vector<uint8_t>& rgba);
 
+// Decodes a JPEG file held in memory (baseline, extended sequential or
+// progressive Huffman, 8-bit, 1 or 3 components) to 8-bit RGB, row 0 at
+// the top. Returns an empty string on success or an error message.
+std::string jpeg_decode(const std::vector<uint8_t>& file, int& width, int& height, std::vector<uint8_t>& rgb);
+
 // zlib stream -> bytes (exposed for tests). Returns "" or an error message.
 std::string zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>& out);
 

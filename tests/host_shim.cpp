@@ -73,6 +73,18 @@ int shim_png_decode(const unsigned char* bytes, long n, int* w, int* h, unsigned
     return 0;
 }
 
+int shim_jpeg_decode(const unsigned char* bytes, long n, int* w, int* h, unsigned char* rgb, char* err, int errlen) {
+    std::vector<uint8_t> f(bytes, bytes + n), out;
+    std::string e = nr::jpeg_decode(f, *w, *h, out);
+    if (!e.empty()) {
+        std::strncpy(err, e.c_str(), (size_t)errlen - 1);
+        err[errlen - 1] = 0;
+        return -1;
+    }
+    if (rgb) std::memcpy(rgb, out.data(), out.size());
+    return 0;
+}
+
 // RGB8 -> PNG bytes; returns the size (out may be null to size it).
 long shim_png_encode(const unsigned char* rgb, int w, int h, unsigned char* out) {
     std::vector<uint8_t> png = nr::png_encode_rgb8(rgb, w, h);

@@ -13,7 +13,7 @@ CSRC = os.path.join(ROOT, "nuray_gb300", "csrc")
 
 def load():
     srcs = [os.path.join(ROOT, "tests", "host_shim.cpp"), os.path.join(CSRC, "host_scene.cpp"),
-            os.path.join(CSRC, "image_io.cpp")]
+            os.path.join(CSRC, "image_io.cpp"), os.path.join(CSRC, "jpeg.cpp")]
     deps = srcs + [os.path.join(CSRC, "host_scene.h"), os.path.join(CSRC, "image_io.h"),
                    os.path.join(ROOT, "include", "nuray.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(p) > os.path.getmtime(LIB) for p in deps):
@@ -30,6 +30,7 @@ def load():
     L.shim_config_vec3.argtypes = [ctypes.c_char_p, ctypes.c_char_p, vp]
     L.shim_camera.argtypes = [ctypes.c_char_p, vp, vp]
     L.shim_png_decode.argtypes = [ctypes.c_char_p, ctypes.c_long, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
+    L.shim_jpeg_decode.argtypes = [ctypes.c_char_p, ctypes.c_long, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
     L.shim_png_encode.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
     L.shim_png_encode.restype = ctypes.c_long
     L.shim_read_image.argtypes = [ctypes.c_char_p, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
@@ -44,6 +45,17 @@ def png_decode(L, data):
         raise ValueError(err.value.decode())
     out = np.zeros((h.value, w.value, 4), np.uint8)
     L.shim_png_decode(data, len(data), ctypes.byref(w), ctypes.byref(h), out.ctypes.data, err, 256)
+    return out
+
+
+def jpeg_decode(L, data):
+    """JPEG bytes -> (h, w, 3) uint8 through the product decoder; raises ValueError."""
+    w, h = ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    if L.shim_jpeg_decode(data, len(data), ctypes.byref(w), ctypes.byref(h), None, err, 256) != 0:
+        raise ValueError(err.value.decode())
+    out = np.zeros((h.value, w.value, 3), np.uint8)
+    L.shim_jpeg_decode(data, len(data), ctypes.byref(w), ctypes.byref(h), out.ctypes.data, err, 256)
     return out
 
 
