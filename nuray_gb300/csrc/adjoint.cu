@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(128) k_shadow_adj(PathState P, DeviceScene S, 
     for (int i = threadIdx.x; i < NG; i += blockDim.x) sg[i] = 0.f;
     __syncthreads();
     GradAcc acc{sg};
-    const uint32_t n = P.counters[CNT_SHADOW];
+    const uint32_t n = min(P.counters[CNT_SHADOW], (uint32_t)P.sh_cap);
     const int lane = threadIdx.x & 31;
     while (true) {
         uint32_t b = 0;

@@ -118,7 +118,10 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // closest hit without postponing too 606.6. With this shape the caps stay
 // best at 10 / 10 (trace 8: 621.8, 12: 629.6; shadow 8: 639.9, 12: 603.1).
 // Also measured and dropped for the shadow rays: dynamic fetch of new rays
-// into idle lanes (Aila and Laine 2009) at 4, 8 or 16 idle lanes, 571.
+// into idle lanes (Aila and Laine 2009) at 4, 8 or 16 idle lanes, 571;
+// the shadow queue sorted by light (counting sort, 257 buckets) before the
+// shadow kernel, 541: rays from neighbouring pixels to different lights
+// share more of their walk than rays to one light from across the frame.
 #ifndef NR_TRACE_MINB
 #define NR_TRACE_MINB 10
 #endif
@@ -179,7 +182,8 @@ __global__ void k_sort_recorded(PathState P, DeviceScene S, int capacity) {
 // has t <= the ray's limit (any_hit); unoccluded rays add their NEE term.
 template <bool COUNT, bool FAST>
 __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, DeviceScene S, float4* t_before) {
-    const uint32_t n = P.counters[CNT_SHADOW];
+    // (a full queue drops rays with an error bit but still counts them)
+    const uint32_t n = min(P.counters[CNT_SHADOW], (uint32_t)P.sh_cap);
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
     while (true) {
