@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--nrc", default=None, metavar="PARAMS",
                     help="each step is a PT + NRC frame: a fresh cache is attached and the render gets "
                          "'nrc=1 nrc_train=16384 PARAMS' (measures the cache's per-frame cost)")
+    ap.add_argument("--params", default="", metavar="KEY=VALUE ...",
+                    help="extra renderer parameters appended to the workload's (e.g. 'tile=2')")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
                     help="c2: the 1M-triangle scene (default); c3: the same with an HDR sky, value-noise "
                          "textures on half the materials and 10%% GGX dielectrics, spp 256; c5: the path-replay "
@@ -98,6 +100,8 @@ def workload(args):
     params = params.replace("spp=64", f"spp={args.spp}").replace("spp=256", f"spp={args.spp}")
     if args.wave:
         params += f" wave={args.wave}"
+    if args.params:
+        params += " " + args.params
     desc = (f"procedural terrain+spheres, {sc['pos'].shape[0]} triangles, {w}x{h}, spp={args.spp}, "
             "maxdepth 8, RR from depth 3, GGX-reflect materials, 32 quad lights, Philox seed 0")
     if args.workload == "c3":

@@ -238,9 +238,12 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * the previous call of the same size instead of clearing it; the outputs are
  * the mean over all samples added so far), sample0 (index of the first
  * sample, default 0: renders of disjoint sample ranges are independent and
- * their films sum), tile (1, the default: the paths of a wave are ordered by
- * 8x4 pixel tiles when imgw % 8 == 0 and imgh % 4 == 0, so a warp's camera
- * rays are coherent; 0: scanline order; the image is the same either way),
+ * their films sum), tile (the order of a wave's paths; the image is the same
+ * for every choice. 2, the default: each warp's 32 paths are tile_samples
+ * consecutive samples of a tile of 32 / tile_samples pixels, tile_samples
+ * by default the largest power of two up to 32 dividing spp, when the tile
+ * divides the image; else 1: 8x4 pixel tiles of one sample when imgw % 8 ==
+ * 0 and imgh % 4 == 0; else or with 0: scanline order),
  * envis=1 (ptnee only, no reference counterpart: one environment light
  * sample per light-sampling vertex besides the area-light sample, weighted
  * against BSDF-sampled misses by the balance heuristic; same expected image),

@@ -54,6 +54,27 @@ __device__ __forceinline__ void frame_pixel(uint32_t p, int w, int tiled, int& x
     }
 }
 
+// tiled == 2: paths come in groups of g_s samples of every pixel; within a
+// group, 32 consecutive paths are samples 0..g_s-1 of a g_w x g_h pixel
+// tile (lane = sample * g_w * g_h + pixel in the tile, row-major), tiles in
+// row-major order.
+__device__ __forceinline__ void tile2_path(const WaveDesc& W, uint64_t g, int w, int& x, int& y, uint32_t& srel) {
+    const uint32_t tp = (uint32_t)(W.g_w * W.g_h);
+    const uint64_t per = (uint64_t)W.g_s * W.npix;
+    const uint32_t grp = (uint32_t)(g / per), l = (uint32_t)(g % per);
+    const uint32_t tile = l >> 5, lane = l & 31u, pit = lane % tp, tiles_x = (uint32_t)w / (uint32_t)W.g_w;
+    x = (int)((tile % tiles_x) * (uint32_t)W.g_w + pit % (uint32_t)W.g_w);
+    y = (int)((tile / tiles_x) * (uint32_t)W.g_h + pit / (uint32_t)W.g_w);
+    srel = grp * (uint32_t)W.g_s + lane / tp;
+}
+// path index of sample srel of the pixel with film-thread index p (p / tile
+// pixels: the tile, the rest: the pixel in it)
+__device__ __forceinline__ uint64_t tile2_index(const WaveDesc& W, uint32_t p, uint32_t srel) {
+    const uint32_t tp = (uint32_t)(W.g_w * W.g_h);
+    return (uint64_t)(srel / (uint32_t)W.g_s) * (uint32_t)W.g_s * W.npix + (uint64_t)(p / tp) * 32u +
+           (srel % (uint32_t)W.g_s) * tp + p % tp;
+}
+
 // ---------------------------------------------------------------- ray generation
 // RendererPTLS::render per-sample body (src/renderer/rendererptls.cpp:170-173):
 // jitter x, jitter y, Camera::generateRay.
@@ -65,6 +86,7 @@ __global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, P
     uint32_t pidx = (uint32_t)(g % (uint64_t)W.npix);
     int x, y;
     if (W.pix_xy) { x = W.pix_xy[2 * pidx]; y = W.pix_xy[2 * pidx + 1]; }
+    else if (W.tiled == 2) tile2_path(W, g, pol.imgw, x, y, srel);
     else frame_pixel(pidx, pol.imgw, W.tiled, x, y);
     uint32_t key = (uint32_t)y * (uint32_t)pol.imgw + (uint32_t)x;
     uint32_t sample = W.sample0 + srel;
@@ -475,9 +497,31 @@ __global__ void k_film(PathState P, WaveDesc W, float4* film, int imgw) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (uint32_t)W.npix) return;
     int x, y;
+    const uint64_t end = W.base + (uint64_t)W.count;
+    if (W.tiled == 2) {
+        const uint32_t tp = (uint32_t)(W.g_w * W.g_h), tile = p / tp, tiles_x = (uint32_t)imgw / (uint32_t)W.g_w;
+        x = (int)((tile % tiles_x) * (uint32_t)W.g_w + (p % tp) % (uint32_t)W.g_w);
+        y = (int)((tile / tiles_x) * (uint32_t)W.g_h + (p % tp) / (uint32_t)W.g_w);
+        const uint32_t pix = (uint32_t)y * (uint32_t)imgw + (uint32_t)x;
+        // this pixel's samples in the wave, in sample order
+        uint32_t s = (uint32_t)(W.base / ((uint64_t)W.g_s * W.npix)) * (uint32_t)W.g_s;
+        float4 acc = film[pix];
+        bool any = false;
+        for (;; ++s) {
+            const uint64_t g = tile2_index(W, p, s);
+            if (g >= end) break;
+            if (g < W.base) continue;
+            const float4 r = P.rad[g - W.base];
+            acc.x += smax(0.f, r.x);
+            acc.y += smax(0.f, r.y);
+            acc.z += smax(0.f, r.z);
+            any = true;
+        }
+        if (any) film[pix] = acc;
+        return;
+    }
     frame_pixel(p, imgw, W.tiled, x, y);
     const uint32_t pix = (uint32_t)y * (uint32_t)imgw + (uint32_t)x;
-    uint64_t end = W.base + (uint64_t)W.count;
     uint64_t s_first = W.base / (uint64_t)W.npix;
     uint64_t g = s_first * (uint64_t)W.npix + p;
     if (g < W.base) g += (uint64_t)W.npix;

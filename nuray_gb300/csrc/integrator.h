@@ -12,7 +12,9 @@ struct WaveDesc {
     int32_t npix;
     uint32_t sample0;
     const int32_t* pix_xy;  // device (x, y) list, or null for the full frame
-    int32_t tiled;          // full frame in 8x4 pixel tiles (frame_pixel)
+    int32_t tiled;          // 0 scanline; 1 full frame in 8x4 pixel tiles (frame_pixel); 2 a warp of paths
+                            // holds g_s consecutive samples of a g_w x g_h pixel tile (g_s g_w g_h = 32)
+    int32_t g_s, g_w, g_h;
 };
 
 void launch_setup(int num_sms);

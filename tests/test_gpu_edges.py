@@ -91,3 +91,21 @@ def test_axis_aligned_rays_match_port(gpu_lib, port_lib):
     assert h.mean() > 0.2
     np.testing.assert_allclose(t_g[h], t_r[h], rtol=1e-5)
     assert np.mean(tri_g[h] != tri_r[h]) < 1e-3
+
+
+def test_wave_layouts_give_the_same_image(gpu_lib):
+    """tile=0 (scanline), 1 (8x4 pixel tiles) and 2 (tile_samples samples of
+    a tile of 32 / tile_samples pixels per warp; by default as many samples
+    as divide spp, up to 32) order the paths differently in the wave; the
+    film adds each pixel's samples in sample order in all of them, also
+    across waves."""
+    S = gpu_scene(cornell_scene())
+    p = CORNELL.replace("spp=4", "spp=16")
+    ref = S.render(p + " tile=0")
+    for extra in (" tile=1", " tile=2", " tile=2 wave=777", " tile=2 wave=4096", " tile=2 wave=12289",
+                  " tile=2 tile_samples=16", " tile=2 tile_samples=4 wave=3001", " tile=2 tile_samples=1",
+                  " tile=2 tile_samples=2 wave=999"):
+        np.testing.assert_array_equal(S.render(p + extra), ref, err_msg=extra)
+    odd = CORNELL.replace("spp=4", "spp=12")
+    for extra in (" tile=2", " tile=2 tile_samples=8"):  # 4 samples per warp; 8 do not divide 12: 8x4 tiles
+        np.testing.assert_array_equal(S.render(odd + extra), S.render(odd + " tile=0"), err_msg=extra)
