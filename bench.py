@@ -247,7 +247,7 @@ def run_adjoint(args, local):
     build.build()
     sc = inverse.c5_scene(0)
     S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"])
-    params = sc["params"]
+    params = sc["params"] + (" " + args.params if args.params else "")
     w = h = 512
     spp = 32
     rng = np.random.default_rng(7)

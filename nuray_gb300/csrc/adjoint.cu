@@ -390,12 +390,14 @@ __device__ void shade_adj(const PathState& P, const DeviceScene& S, const Policy
 
 // Per wave, after ray generation: each path's radiance and gradient weight;
 // paths whose gradient weight is zero are left out of the queue.
-__global__ void k_adj_init(PathState P, AdjWave J, uint64_t base, int count, int npix, int spp,
-                           const float* __restrict__ Lbuf, const float* __restrict__ dldi) {
+__global__ void k_adj_init(PathState P, AdjWave J, WaveDesc W, int imgw, int spp, const float* __restrict__ Lbuf,
+                           const float* __restrict__ dldi) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const uint64_t g = base + (uint64_t)i;
-    const uint64_t pidx = g % (uint64_t)npix, srel = g / (uint64_t)npix;
+    if (i >= W.count) return;
+    int x, y;
+    uint32_t srel;
+    wave_path(W, W.base + (uint64_t)i, imgw, x, y, srel);
+    const uint64_t pidx = (uint64_t)y * (uint64_t)imgw + (uint64_t)x;
     const float* l = Lbuf + (pidx * (uint64_t)spp + srel) * 3;
     const float inv = 1.0f / (float)spp;
     const f3 d = mk(l[0] > 0.f ? dldi[3 * pidx] * inv : 0.f, l[1] > 0.f ? dldi[3 * pidx + 1] * inv : 0.f,
@@ -473,9 +475,9 @@ __global__ void __launch_bounds__(128) k_shadow_adj(PathState P, DeviceScene S, 
         if (sg[i] != 0.f) atomicAdd(&grad[i], sg[i]);
 }
 
-void launch_adj_init(const PathState& P, const AdjWave& J, uint64_t base, int count, int npix, int spp,
-                     const float* Lbuf, const float* dldi, cudaStream_t st) {
-    k_adj_init<<<(count + 255) / 256, 256, 0, st>>>(P, J, base, count, npix, spp, Lbuf, dldi);
+void launch_adj_init(const PathState& P, const AdjWave& J, const WaveDesc& W, int imgw, int spp, const float* Lbuf,
+                     const float* dldi, cudaStream_t st) {
+    k_adj_init<<<(W.count + 255) / 256, 256, 0, st>>>(P, J, W, imgw, spp, Lbuf, dldi);
     k_adj_setin<<<1, 1, 0, st>>>(P.counters);
 }
 int launch_adj_bounce_shading(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity,

@@ -1,5 +1,6 @@
 // Path-replay adjoint (adjoint.cu).
 #pragma once
+#include "integrator.h"
 #include "nr_types.h"
 
 namespace nr {
@@ -27,8 +28,10 @@ struct AdjWave {
     float4* sg0;
     float4* sg1;
 };
-void launch_adj_init(const PathState& P, const AdjWave& J, uint64_t base, int count, int npix, int spp,
-                     const float* Lbuf, const float* dldi, cudaStream_t st);
+// W: the wave (its layout as rendered); the radiance buffer and dldi are
+// indexed by scanline pixel, Lbuf as (pixel * spp + sample) * 3.
+void launch_adj_init(const PathState& P, const AdjWave& J, const WaveDesc& W, int imgw, int spp, const float* Lbuf,
+                     const float* dldi, cudaStream_t st);
 // Shading of one bounce (after launch_trace or launch_sort_recorded), adding
 // to grad. vis: the bounce's light-sample visibility recorded by the first
 // pass, or null to trace the shadow rays here. Returns the kernels launched.

@@ -504,6 +504,19 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
 // Traces all paths of [0, npix * spp) in waves. Per wave: ray generation,
 // then trace/shade/shadow bounces until no path is live, then either the
 // film accumulation (film != null) or the per-sample copy (out != null).
+// The order of a wave's paths (RenderArgs::tile): tiles of tile_samples
+// samples where they divide the frame and spp, else 8x4 pixel tiles, else
+// scanline; a pixel list is always in list order.
+void wave_layout(const RenderArgs& A, bool has_pix_list, nr::WaveDesc& W) {
+    W.tiled = 0;
+    W.g_s = A.tile_samples;
+    W.g_w = W.g_s >= 16 ? 32 / W.g_s : (W.g_s >= 4 ? 16 / W.g_s : 4);  // 32 / g_s pixels, as square as fits
+    W.g_h = 32 / (W.g_s * W.g_w);
+    if (has_pix_list) return;
+    if (A.tile == 2 && A.pol.imgw % W.g_w == 0 && A.pol.imgh % W.g_h == 0 && A.spp % W.g_s == 0) W.tiled = 2;
+    else if (A.tile >= 1 && A.pol.imgw % 8 == 0 && A.pol.imgh % 4 == 0) W.tiled = 1;
+}
+
 void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pix, int sample0, float4* film,
                float* dev_out, volatile int32_t* cancel, void (*progress)(float, void*), void* user) {
     const uint64_t total = (uint64_t)npix * (uint64_t)A.spp;
@@ -581,13 +594,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         W.npix = npix;
         W.sample0 = (uint32_t)sample0;
         W.pix_xy = dev_pix;
-        W.tiled = 0;
-        W.g_s = A.tile_samples;
-        W.g_w = W.g_s >= 16 ? 32 / W.g_s : (W.g_s >= 4 ? 16 / W.g_s : 4);  // 32/s pixels, as square as fits
-        W.g_h = 32 / (W.g_s * W.g_w);
-        if (!dev_pix && A.tile == 2 && A.pol.imgw % W.g_w == 0 && A.pol.imgh % W.g_h == 0 && A.spp % W.g_s == 0)
-            W.tiled = 2;
-        else if (!dev_pix && A.tile >= 1 && A.pol.imgw % 8 == 0 && A.pol.imgh % 4 == 0) W.tiled = 1;
+        wave_layout(A, dev_pix != nullptr, W);
         mark(-1);
         // queue_in / queue_out swap roles every bounce
         nr::PathState P = s->ps;
@@ -656,7 +663,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         }
         mark(-1);
         if (film) nr::launch_film(s->ps, W, film, A.pol.imgw, st);
-        if (dev_out) nr::launch_collect(s->ps, W, dev_out, A.spp, st);
+        if (dev_out) nr::launch_collect(s->ps, W, dev_out, A.spp, A.pol.imgw, st);
         S.kernel_launches += 1;
         mark(3);
         S.waves++;
@@ -745,10 +752,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
         W.npix = npix;
         W.sample0 = (uint32_t)A.sample0;
         W.pix_xy = nullptr;
-        W.tiled = 0;
-        W.g_s = 1;
-        W.g_w = 8;
-        W.g_h = 4;
+        wave_layout(A, false, W);
         // pass 1
         nr::PathState P = s->ps;
         nr::launch_reset_counters(P.counters, st);
@@ -765,12 +769,12 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
             launches += 4;
             if (!live_after(bounce, live)) break;
         }
-        nr::launch_collect(s->ps, W, s->adj_L.as<float>(), A.spp, st);
+        nr::launch_collect(s->ps, W, s->adj_L.as<float>(), A.spp, A.pol.imgw, st);
         // pass 2
         P = s->ps;
         nr::launch_reset_counters(P.counters, st);
         nr::launch_raygen(P, W, A.cam, film_h, A.pol, st);
-        nr::launch_adj_init(P, J, base, W.count, npix, A.spp, s->adj_L.as<float>(), d_dldi, st);
+        nr::launch_adj_init(P, J, W, A.pol.imgw, A.spp, s->adj_L.as<float>(), d_dldi, st);
         launches += 5;
         live = W.count;
         for (int bounce = 0;; ++bounce) {

@@ -41,40 +41,6 @@ __device__ __forceinline__ int warp_append_keyed(int key, uint32_t* counters) {
     return (int)(base + rank);
 }
 
-// Full-frame pixel of path index p: row-major, or in 8x4 tiles (one warp of
-// consecutive paths covers a compact patch) when the frame divides into them.
-__device__ __forceinline__ void frame_pixel(uint32_t p, int w, int tiled, int& x, int& y) {
-    if (tiled) {
-        uint32_t tile = p >> 5, j = p & 31u, tiles_x = (uint32_t)w >> 3;
-        x = (int)((tile % tiles_x) * 8u + (j & 7u));
-        y = (int)((tile / tiles_x) * 4u + (j >> 3));
-    } else {
-        x = (int)(p % (uint32_t)w);
-        y = (int)(p / (uint32_t)w);
-    }
-}
-
-// tiled == 2: paths come in groups of g_s samples of every pixel; within a
-// group, 32 consecutive paths are samples 0..g_s-1 of a g_w x g_h pixel
-// tile (lane = sample * g_w * g_h + pixel in the tile, row-major), tiles in
-// row-major order.
-__device__ __forceinline__ void tile2_path(const WaveDesc& W, uint64_t g, int w, int& x, int& y, uint32_t& srel) {
-    const uint32_t tp = (uint32_t)(W.g_w * W.g_h);
-    const uint64_t per = (uint64_t)W.g_s * W.npix;
-    const uint32_t grp = (uint32_t)(g / per), l = (uint32_t)(g % per);
-    const uint32_t tile = l >> 5, lane = l & 31u, pit = lane % tp, tiles_x = (uint32_t)w / (uint32_t)W.g_w;
-    x = (int)((tile % tiles_x) * (uint32_t)W.g_w + pit % (uint32_t)W.g_w);
-    y = (int)((tile / tiles_x) * (uint32_t)W.g_h + pit / (uint32_t)W.g_w);
-    srel = grp * (uint32_t)W.g_s + lane / tp;
-}
-// path index of sample srel of the pixel with film-thread index p (p / tile
-// pixels: the tile, the rest: the pixel in it)
-__device__ __forceinline__ uint64_t tile2_index(const WaveDesc& W, uint32_t p, uint32_t srel) {
-    const uint32_t tp = (uint32_t)(W.g_w * W.g_h);
-    return (uint64_t)(srel / (uint32_t)W.g_s) * (uint32_t)W.g_s * W.npix + (uint64_t)(p / tp) * 32u +
-           (srel % (uint32_t)W.g_s) * tp + p % tp;
-}
-
 // ---------------------------------------------------------------- ray generation
 // RendererPTLS::render per-sample body (src/renderer/rendererptls.cpp:170-173):
 // jitter x, jitter y, Camera::generateRay.
@@ -83,11 +49,10 @@ __global__ void k_raygen(PathState P, WaveDesc W, nr_camera cam, float film_h, P
     if (i >= W.count) return;
     uint64_t g = W.base + (uint64_t)i;
     uint32_t srel = (uint32_t)(g / (uint64_t)W.npix);
-    uint32_t pidx = (uint32_t)(g % (uint64_t)W.npix);
+    const uint32_t pidx = (uint32_t)(g % (uint64_t)W.npix);
     int x, y;
     if (W.pix_xy) { x = W.pix_xy[2 * pidx]; y = W.pix_xy[2 * pidx + 1]; }
-    else if (W.tiled == 2) tile2_path(W, g, pol.imgw, x, y, srel);
-    else frame_pixel(pidx, pol.imgw, W.tiled, x, y);
+    else wave_path(W, g, pol.imgw, x, y, srel);
     uint32_t key = (uint32_t)y * (uint32_t)pol.imgw + (uint32_t)x;
     uint32_t sample = W.sample0 + srel;
     Stream s;
@@ -536,12 +501,20 @@ __global__ void k_film(PathState P, WaveDesc W, float4* film, int imgw) {
     film[pix] = acc;
 }
 
-// Copies per-sample max(0, L) to out[(pixel * spp + sample) * 3].
-__global__ void k_collect(PathState P, WaveDesc W, float* out, int spp) {
+// Copies per-sample max(0, L) to out[(pixel * spp + sample) * 3], pixel the
+// index in the pixel list, or y * imgw + x for a full frame.
+__global__ void k_collect(PathState P, WaveDesc W, float* out, int spp, int imgw) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= W.count) return;
     uint64_t g = W.base + (uint64_t)i;
     uint64_t srel = g / (uint64_t)W.npix, pidx = g % (uint64_t)W.npix;
+    if (!W.pix_xy && W.tiled) {
+        int x, y;
+        uint32_t s;
+        wave_path(W, g, imgw, x, y, s);
+        srel = s;
+        pidx = (uint64_t)y * (uint64_t)imgw + (uint64_t)x;
+    }
     float4 r = P.rad[i];
     float* o = out + (pidx * (uint64_t)spp + srel) * 3;
     o[0] = smax(0.f, r.x); o[1] = smax(0.f, r.y); o[2] = smax(0.f, r.z);
@@ -698,8 +671,8 @@ void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, 
     k_film<<<(W.npix + 255) / 256, 256, 0, st>>>(P, W, film, imgw);
 }
 
-void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st) {
-    k_collect<<<(W.count + 255) / 256, 256, 0, st>>>(P, W, out, spp);
+void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, int imgw, cudaStream_t st) {
+    k_collect<<<(W.count + 255) / 256, 256, 0, st>>>(P, W, out, spp, imgw);
 }
 
 void launch_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8, cudaStream_t st) {

@@ -17,6 +17,53 @@ struct WaveDesc {
     int32_t g_s, g_w, g_h;
 };
 
+#ifdef __CUDACC__
+// Full-frame pixel of path index p: row-major, or in 8x4 tiles (one warp of
+// consecutive paths covers a compact patch) when the frame divides into them.
+__device__ __forceinline__ void frame_pixel(uint32_t p, int w, int tiled, int& x, int& y) {
+    if (tiled) {
+        uint32_t tile = p >> 5, j = p & 31u, tiles_x = (uint32_t)w >> 3;
+        x = (int)((tile % tiles_x) * 8u + (j & 7u));
+        y = (int)((tile / tiles_x) * 4u + (j >> 3));
+    } else {
+        x = (int)(p % (uint32_t)w);
+        y = (int)(p / (uint32_t)w);
+    }
+}
+
+// tiled == 2: paths come in groups of g_s samples of every pixel; within a
+// group, 32 consecutive paths are samples 0..g_s-1 of a g_w x g_h pixel
+// tile (lane = sample * g_w * g_h + pixel in the tile, row-major), tiles in
+// row-major order.
+__device__ __forceinline__ void tile2_path(const WaveDesc& W, uint64_t g, int w, int& x, int& y, uint32_t& srel) {
+    const uint32_t tp = (uint32_t)(W.g_w * W.g_h);
+    const uint64_t per = (uint64_t)W.g_s * W.npix;
+    const uint32_t grp = (uint32_t)(g / per), l = (uint32_t)(g % per);
+    const uint32_t tile = l >> 5, lane = l & 31u, pit = lane % tp, tiles_x = (uint32_t)w / (uint32_t)W.g_w;
+    x = (int)((tile % tiles_x) * (uint32_t)W.g_w + pit % (uint32_t)W.g_w);
+    y = (int)((tile / tiles_x) * (uint32_t)W.g_h + pit / (uint32_t)W.g_w);
+    srel = grp * (uint32_t)W.g_s + lane / tp;
+}
+// path index of sample srel of the pixel with film-thread index p (p / tile
+// pixels: the tile, the rest: the pixel in it)
+__device__ __forceinline__ uint64_t tile2_index(const WaveDesc& W, uint32_t p, uint32_t srel) {
+    const uint32_t tp = (uint32_t)(W.g_w * W.g_h);
+    return (uint64_t)(srel / (uint32_t)W.g_s) * (uint32_t)W.g_s * W.npix + (uint64_t)(p / tp) * 32u +
+           (srel % (uint32_t)W.g_s) * tp + p % tp;
+}
+
+// Pixel (x, y) of wave path g (global index) and its sample relative to
+// sample0, for a wave without a pixel list.
+__device__ __forceinline__ void wave_path(const WaveDesc& W, uint64_t g, int imgw, int& x, int& y, uint32_t& srel) {
+    if (W.tiled == 2) {
+        tile2_path(W, g, imgw, x, y, srel);
+        return;
+    }
+    srel = (uint32_t)(g / (uint64_t)W.npix);
+    frame_pixel((uint32_t)(g % (uint64_t)W.npix), imgw, W.tiled, x, y);
+}
+#endif
+
 void launch_setup(int num_sms);
 void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
                    cudaStream_t st);
@@ -35,7 +82,7 @@ void launch_advance(uint32_t* counters, cudaStream_t st);
 void launch_sort_recorded(const PathState& P, const DeviceScene& S, int capacity, cudaStream_t st);
 int shadow_grid();  // blocks of the persistent shadow-ray kernels
 void launch_film(const PathState& P, const WaveDesc& W, float4* film, int imgw, cudaStream_t st);
-void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, cudaStream_t st);
+void launch_collect(const PathState& P, const WaveDesc& W, float* out, int spp, int imgw, cudaStream_t st);
 void launch_finish(const float4* film, int npix, float inv_spp, float* hdr, uint8_t* rgb8, cudaStream_t st);
 void launch_intersect(const DeviceScene& S, int n, const float* o, const float* d, int* tri, float* t, float* b1,
                       float* b2, uint32_t* err, cudaStream_t st);
