@@ -191,20 +191,30 @@ def cpu_leg(sc, params, spp, w, h, stride, budget_s=20.0):
     return n * spp / dt / 1e6, desc, threads
 
 
-def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0):
+def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0, spf=64):
     """Second half of the metric: wall time (CUDA events) to relMSE <= 1e-3
     against a converged render, plain PT against PT + the online neural
-    radiance cache, both progressive at one sample per pixel per frame."""
+    radiance cache, both progressive with the same frame size: `spf`
+    samples per pixel per frame (64: near the fastest frame size of either
+    method on this scene), and one sample per pixel per frame (the
+    real-time regime, where fixed per-frame costs weigh most)."""
     from nuray_gb300 import convergence as C
     w, h = res.split("x")
     p = params.replace("imgw=1920", f"imgw={w}").replace("imgh=1080", f"imgh={h}")
     ref = C.reference(S, p, ref_spp)
-    pt_curve, pt_t = C.progressive(S, p, 100000, ref, target, time_limit_s=limit_s)
-    nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "nrc_train=16384", limit_s)
-    return {"target": target, "resolution": res, "reference_spp": ref_spp, "unit": "ms",
-            "pt": C.summary(pt_curve, pt_t), "pt_nrc": C.summary(nrc_curve, nrc_t),
-            "note": "GPU time (CUDA events) of the frames up to the first checkpoint at or below the target; "
-                    "None when not reached within the time limit"}
+    out = {"target": target, "resolution": res, "reference_spp": ref_spp, "unit": "ms", "spp_per_frame": spf}
+    for k, label in ((spf, None), (1, "at_1_spp_per_frame")):
+        pt_curve, pt_t = C.progressive(S, p, 100000, ref, target, time_limit_s=limit_s, spf=k)
+        nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "nrc_train=16384", limit_s, warmup=max(1, 256 // k),
+                                     spf=k)
+        res_k = {"pt": C.summary(pt_curve, pt_t), "pt_nrc": C.summary(nrc_curve, nrc_t)}
+        if label:
+            out[label] = res_k
+        else:
+            out.update(res_k)
+    out["note"] = ("GPU time (CUDA events) of the frames up to the first checkpoint at or below the target; "
+                   "'spp' is the samples per pixel at that checkpoint; None when not reached within the time limit")
+    return out
 
 
 def run_reference(args, rank, world):

@@ -1,6 +1,6 @@
 """Time to a relMSE target: plain GPU path tracing against PT + the online
-neural radiance cache, both progressive (one sample per pixel per frame)
-on the same scene and GPU.
+neural radiance cache, both progressive (frames of `spf` samples per pixel,
+accumulated) on the same scene and GPU.
 
 relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2) on linear
 HDR with FP64 sums, R a high-sample plain render with an independent seed.
@@ -20,8 +20,9 @@ def relmse(img, ref):
 
 
 def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", time_limit_s=60.0, growth=1.03,
-                warmup=0):
-    """Renders up to `frames` 1-spp frames, accumulated on the device; the
+                warmup=0, spf=1):
+    """Renders up to `frames` frames of `spf` samples per pixel (default 1),
+    accumulated on the device; the
     image is read back and compared at checkpoints spaced by `growth` in
     sample count. With a cache, the first `warmup` frames are plain path
     tracing that only trains it (unbiased samples that count towards the
@@ -36,7 +37,7 @@ def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", tim
     next_check = 1.0
     t_wall = time.perf_counter()
     for k in range(frames):
-        p = params.replace("spp=", "spp_unused=") + f" spp=1 sample0={k}" + (" accumulate=1" if k else "")
+        p = params.replace("spp=", "spp_unused=") + f" spp={spf} sample0={k * spf}" + (" accumulate=1" if k else "")
         if nrc is not None:
             p += " nrc=1 " + nrc_params + (" nrc_query=0" if k < warmup else "")
         check = k + 1 >= next_check or k == frames - 1
@@ -49,7 +50,7 @@ def progressive(scene, params, frames, ref, target, nrc=None, nrc_params="", tim
         if check:
             next_check = max(next_check * growth, k + 2)
             err = relmse(img, ref)
-            curve.append((round(elapsed, 2), k + 1, err))
+            curve.append((round(elapsed, 2), (k + 1) * spf, err))
             if err <= target:
                 hit = elapsed
                 break
@@ -62,21 +63,21 @@ def reference(scene, params, ref_spp=8192, seed_ref=12345):
     return scene.render(params.replace("spp=", "spp_unused=") + f" spp={ref_spp} seed={seed_ref}")
 
 
-def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s, warmup=256):
+def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s, warmup=256, spf=1):
     from ._lib import check, lib
     from .nrc import Cache
     cache = Cache("lr=1e-3 beta1=0.9 beta2=0.99")
     cache.attach(scene)
     try:
         return progressive(scene, params, frames, ref, target, nrc=cache, nrc_params=nrc_params,
-                           time_limit_s=time_limit_s, warmup=warmup)
+                           time_limit_s=time_limit_s, warmup=warmup, spf=spf)
     finally:
         check(lib().nr_scene_attach_nrc(scene._h, None))
         cache.close()
 
 
 def summary(curve, t):
-    return {"ms_to_target": None if t is None else round(t, 1), "frames": curve[-1][1], "final_relmse": curve[-1][2]}
+    return {"ms_to_target": None if t is None else round(t, 1), "spp": curve[-1][1], "final_relmse": curve[-1][2]}
 
 
 def compare(scene, params, target=1e-3, ref_spp=8192, frames=50000, nrc_params="nrc_train=16384", time_limit_s=60.0):
