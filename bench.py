@@ -48,7 +48,7 @@ BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry
 # DRAM bytes (read + write) per closest-hit ray of k_trace, from one ncu
 # capture of a bounce-0 launch (profiles/k_trace_c2_first_bounce.md); the
 # roofline's `traffic` scales it to a full launch by rays per launch.
-TRACE_DRAM_BYTES_PER_RAY = 129.2
+TRACE_DRAM_BYTES_PER_RAY = 62.3
 
 
 def parse():
