@@ -418,6 +418,13 @@ struct RenderArgs {
     // their first bounces stay close, so a warp walks much of the same tree.
     int tile;
     int tile_samples;     // 1, 2, 4, 8, 16 or 32
+    // With maxdepth: the bounces after which the live count is read back, so
+    // that later bounces size the shading grid to the paths left (0: never;
+    // -1, the default: 5 for waves of more than 2^22 paths, else never).
+    // 1M-triangle scene: 1080p x 64 spp 704.3 Mpaths/s with the readback
+    // against 699.0 without; 960x540 frames of 1 spp 2.789 ms with it,
+    // 2.735 without (the wait costs more than the grid saves).
+    int live_sync;
     bool nrc;
     int nrc_train;    // training paths per wavefront batch
     int nrc_steps;    // Adam steps per batch
@@ -466,6 +473,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.accumulate = c.get_int("accumulate", 0) != 0;
     a.tile = c.get_int("tile", 2);
     if (a.tile < 0 || a.tile > 2) throw NrError(NR_ERR_INVALID, "tile must be 0, 1 or 2");
+    a.live_sync = c.get_int("live_sync", -1);
     // 0: the largest power of two up to 32 that divides spp
     a.tile_samples = c.get_int("tile_samples", 0);
     if (a.tile_samples < 0 || a.tile_samples > 32 || (a.tile_samples & (a.tile_samples - 1)))
@@ -586,6 +594,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
     };
     NR_CUDA(cudaMemsetAsync(s->ps.counters, 0, nr::NUM_COUNTERS * 4, st));
     S.kernel_launches = 0;
+    const int live_sync = A.live_sync >= 0 ? A.live_sync : (cap > (1 << 22) ? 5 : 0);
     for (uint64_t base = 0; base < total; base += (uint64_t)cap) {
         if (cancel && *cancel == 0) throw NrError(NR_ERR_CANCELLED, "cancelled");
         nr::WaveDesc W;
@@ -625,7 +634,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             S.kernel_launches += 4;
             // With a depth limit the loop runs exactly maxdepth bounces; without
             // one the live count is read back to find the end of the wave.
-            if (A.pol.maxdepth == 0 || bounce >= 4) {
+            if (A.pol.maxdepth == 0 || (live_sync > 0 && bounce + 1 >= live_sync)) {
                 NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters, nr::NUM_COUNTERS * 4, cudaMemcpyDeviceToHost, st));
                 NR_CUDA(cudaStreamSynchronize(st));
                 live = (int)s->counters_host[nr::CNT_IN];

@@ -625,6 +625,9 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
         default: k_trace<true, true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
     }
     if (ev) cudaEventRecord(ev[1], st);
+    // k_shade strides over the device count; max_count (an upper bound of
+    // it) sizes the grid, one thread per path (capping the grid at 4 or 16
+    // resident rounds of blocks measured 693-695 against 704 Mpaths/s)
     int shade_blocks = (max_count + 127) / 128;
     if (shade_blocks < 1) shade_blocks = 1;
     if (nrc) k_shade<true><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, *nrc);
