@@ -134,13 +134,7 @@ __device__ f3 replay(const AdjArgs& A, uint32_t key, uint32_t sample, int x, int
         dfac_da = 0.f;
         prev_m = m;
         if (pol.nee && mat_nee(type) && S.num_lights > 0) {
-            float r = rng.next();
-            int lo = 0, hi = S.num_lights;
-            while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                if (__ldg(&S.light_cdf[mid]) < r) lo = mid + 1; else hi = mid;
-            }
-            int li = lo < S.num_lights ? lo : S.num_lights - 1;
+            const int li = pick_light(S, rng.next());
             const float4* L = S.lights + 6 * li;
             float4 l0 = __ldg(&L[0]), l1 = __ldg(&L[1]), l2 = __ldg(&L[2]);
             float4 n0 = __ldg(&L[3]), n1 = __ldg(&L[4]), n2 = __ldg(&L[5]);
@@ -294,13 +288,7 @@ __device__ void shade_adj(const PathState& P, const DeviceScene& S, const Policy
     const int depth = (int)(meta.w & NR_META_DEPTH_MASK);
     float fac = 1.f, dfac_da = 0.f;
     if (pol.nee && mat_nee(type) && S.num_lights > 0) {
-        const float r = rng.next();
-        int lo = 0, hi = S.num_lights;
-        while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (__ldg(&S.light_cdf[mid]) < r) lo = mid + 1; else hi = mid;
-        }
-        const int li = lo < S.num_lights ? lo : S.num_lights - 1;
+        const int li = pick_light(S, rng.next());
         const float4* Lt = S.lights + 6 * li;
         const float4 l0 = __ldg(&Lt[0]), l1 = __ldg(&Lt[1]), l2 = __ldg(&Lt[2]);
         const float4 n0 = __ldg(&Lt[3]), n1 = __ldg(&Lt[4]), n2 = __ldg(&Lt[5]);

@@ -121,7 +121,7 @@ struct nr_scene {
     nr::HostScene host;
     nr::Bvh bvh;
     nr::DeviceScene dev{};
-    DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_mat;
+    DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_guide, light_mat;
     DevBuf adj_L;  // per-path radiance for the adjoint replay
     DevBuf adj_wave;  // per-slot state of the wavefront adjoint replay
     DevBuf env_weight, env_row_cdf, env_col_cdf;  // environment sampling table (envis=1)
@@ -147,7 +147,7 @@ struct nr_scene {
     ~nr_scene() {
         if (device >= 0) cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
-        for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_mat, &path_mem,
+        for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_guide, &light_mat, &path_mem,
                         &film, &out_hdr, &out_rgb8, &pix_list, &scratch, &nrc_mem})
             b->release();
         if (counters_host) cudaFreeHost(counters_host);
@@ -161,7 +161,7 @@ namespace {
 uint64_t device_bytes(const nr_scene* s) {
     uint64_t b = 0;
     for (auto* x : {&s->nodes, &s->tri_geo, &s->tri_shade, &s->mats, &s->texels, &s->tex_info, &s->lights, &s->light_cdf,
-                    &s->light_mat})
+                    &s->light_guide, &s->light_mat})
         b += x->bytes;
     return b;
 }
@@ -249,6 +249,17 @@ void upload_scene(nr_scene* s) {
     std::vector<float> cdf;
     float acc = 1e-6f;
     for (float& x : pdf) { x /= sum; acc += x; cdf.push_back(acc); }
+    // Guide table of the CDF: entry b is lower_bound(cdf, b / K) for a power
+    // of two K (twice the emitters, at most 2^16), so the device's lower_bound
+    // of r searches only between entries floor(r K) and floor(r K) + 1 (r K
+    // is exact in float) and returns the index the full search returns.
+    int guide_k = 1;
+    while (guide_k < 2 * (int)cdf.size() && guide_k < (1 << 16)) guide_k *= 2;
+    std::vector<int32_t> guide(guide_k + 1);
+    for (int b = 0; b <= guide_k; ++b) {
+        const float u = (float)b / (float)guide_k;
+        guide[b] = (int32_t)(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+    }
 
     std::vector<float4> texels;
     std::vector<int4> tinfo;
@@ -274,6 +285,7 @@ void upload_scene(nr_scene* s) {
     upload(s->tex_info, tinfo, st);
     upload(s->lights, lt, st);
     upload(s->light_cdf, cdf, st);
+    upload(s->light_guide, guide, st);
     upload(s->light_mat, lmat, st);
     upload(s->env_weight, env_table.weight, st);
     upload(s->env_row_cdf, env_table.row_cdf, st);
@@ -289,6 +301,8 @@ void upload_scene(nr_scene* s) {
     D.tex_info = s->tex_info.as<int4>();
     D.lights = s->lights.as<float4>();
     D.light_cdf = s->light_cdf.as<float>();
+    D.light_guide = s->light_guide.as<int32_t>();
+    D.light_guide_k = guide_k;
     D.light_mat = s->light_mat.as<int32_t>();
     D.env_weight = env_table.w ? s->env_weight.as<float>() : nullptr;
     D.env_row_cdf = env_table.w ? s->env_row_cdf.as<float>() : nullptr;

@@ -324,14 +324,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     // next-event estimation (rendererptls.cpp:49-78)
     if (pol.excl && pol.nee && mat_nee(type)) fac = 0.0f;  // is_light_sampled (renderernrc.cpp:139)
     if (pol.nee && mat_nee(type) && S.num_lights > 0) {
-        float r = rng.next();
-        // LightSampler::sampleLight: lower_bound over the CDF
-        int lo = 0, hi = S.num_lights;
-        while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (__ldg(&S.light_cdf[mid]) < r) lo = mid + 1; else hi = mid;
-        }
-        int li = lo < S.num_lights ? lo : S.num_lights - 1;
+        const int li = pick_light(S, rng.next());
         const float4* L = S.lights + 6 * li;
         float4 l0 = __ldg(&L[0]), l1 = __ldg(&L[1]), l2 = __ldg(&L[2]);
         float4 n0 = __ldg(&L[3]), n1 = __ldg(&L[4]), n2 = __ldg(&L[5]);

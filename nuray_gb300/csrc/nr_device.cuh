@@ -226,6 +226,22 @@ __device__ __forceinline__ bool tri_test_fast(f3 o, f3 d, float4 g0, float4 g1, 
 // determinant (q + 1e-6) shortens t by a factor q / (q + 1e-6), so a
 // triangle can report a t slightly below its box's entry distance; the
 // margin keeps such triangles reachable unless |q| < 1e-6 / margin.
+// LightSampler::sampleLight (src/sampler/lightsampler.cpp:56): the first
+// emitter whose CDF entry is >= r (lower_bound), or the last one. The guide
+// table narrows the search to the emitters between the lower bounds of
+// floor(r K) / K and (floor(r K) + 1) / K, which enclose the answer.
+__device__ __forceinline__ int pick_light(const DeviceScene& S, float r) {
+    const int k = S.light_guide_k;
+    int b = (int)(r * (float)k);
+    b = b < 0 ? 0 : (b > k - 1 ? k - 1 : b);
+    int lo = __ldg(&S.light_guide[b]), hi = __ldg(&S.light_guide[b + 1]);
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&S.light_cdf[mid]) < r) lo = mid + 1; else hi = mid;
+    }
+    return lo < S.num_lights ? lo : S.num_lights - 1;
+}
+
 #define NR_PRUNE_MARGIN 1e-3f
 #define NR_STACK NR_STACK_LIMIT
 

@@ -43,6 +43,8 @@ struct DeviceScene {
     const int4* tex_info;     // (w, h, texel offset, 0)
     const float4* lights;     // 6 per emitter: (p0, Ke.x) (p1, Ke.y) (p2, Ke.z) (n0,0) (n1,0) (n2,0)
     const float* light_cdf;
+    const int32_t* light_guide;  // light_guide_k + 1 entries: lower_bound(light_cdf, b / light_guide_k)
+    int32_t light_guide_k;       // a power of two
     const int32_t* light_mat;  // material index of each emitter
     int32_t num_lights;
     float light_p;            // LightSampler::p()
