@@ -193,19 +193,28 @@ __device__ __forceinline__ bool tri_test(f3 o, f3 d, float4 g0, float4 g1, float
 __device__ __forceinline__ bool tri_test_fast(f3 o, f3 d, float4 g0, float4 g1, float4 g2, float limit, float& t,
                                               float& b1, float& b2) {
     f3 p0 = xyz(g0), e1 = xyz(g1), e2 = xyz(g2);
-    f3 s = rsub3(o, p0);
+    const float e = 1e-6f, tiny = 1e-30f;
+    // The rejections in the order of what they need, so a miss on the first
+    // barycentric skips the second cross product: the same rejections as the
+    // exact test's, all of them checked before a hit is kept (1M-triangle
+    // frame: 706.1 -> 717.1 Mpaths/s against computing all before rejecting).
     f3 s1 = rcross(d, e2);
     float q = add_1e6(rdot(s1, e1));
+    f3 s = rsub3(o, p0);
+    float u = rdot(s1, s);
+    // quotients from an approximate reciprocal (2 ulp): within 2^-21 of the exact ones
+    float rq = __fdividef(1.0f, q);
+    float ua = u * rq;
+    if (ua < -tiny) return false;
     f3 s2 = rcross(s, e1);
+    float v = rdot(s2, d);
+    float va = v * rq;
+    if (va < -tiny || ua + va > 1.0f + 2.0f * e) return false;
     float tt = rdot(s2, e2);
     // t = tt / q > 0 needs equal signs and tt != 0 (exact)
     if (tt == 0.0f || ((__float_as_uint(tt) ^ __float_as_uint(q)) & 0x80000000u)) return false;
-    float u = rdot(s1, s), v = rdot(s2, d);
-    // quotients from an approximate reciprocal (2 ulp): within 2^-21 of the exact ones
-    float rq = __fdividef(1.0f, q);
-    float ta = tt * rq, ua = u * rq, va = v * rq;
-    const float e = 1e-6f, tiny = 1e-30f;
-    if (ta > limit * (1.0f + e) || ua < -tiny || va < -tiny || ua + va > 1.0f + 2.0f * e) return false;
+    float ta = tt * rq;
+    if (ta > limit * (1.0f + e)) return false;
     float rqe = __frcp_rn(q);
     if (ta < limit * (1.0f - e) && ta > tiny && ua > tiny && va > tiny && ua + va < 1.0f - 2.0f * e) {
         t = qdiv(tt, q, rqe);
