@@ -205,7 +205,8 @@ __device__ __forceinline__ bool tri_test_fast(f3 o, f3 d, float4 g0, float4 g1, 
     // quotients from an approximate reciprocal (2 ulp): within 2^-21 of the exact ones
     float rq = __fdividef(1.0f, q);
     float ua = u * rq;
-    if (ua < -tiny) return false;
+    // with va >= -tiny, ua > 1 + 2e already puts the rounded ua + va above 1 + 2e
+    if (ua < -tiny || ua > 1.0f + 2.0f * e) return false;
     f3 s2 = rcross(s, e1);
     float v = rdot(s2, d);
     float va = v * rq;
@@ -479,7 +480,10 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
             bool h1 = (FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1)) && t1 <= lim;
             if (h0 && h1) {
                 int nr = k.x, fr = k.y;
-                if (t1 < t0) { nr = k.y; fr = k.x; }
+                // far child first: the near one holds the surface the shadow
+                // ray leaves and its neighbours, which seldom occlude it
+                // (1M-triangle frame: 722.5 Mpaths/s near first, 759.8 far first)
+                if (t1 > t0) { nr = k.y; fr = k.x; }
                 if (sp >= NR_STACK) { atomicOr(err, 1u); return false; }
                 stack[sp++] = fr;
                 ref = nr;
