@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(128) k_shadow_adj(PathState P, DeviceScene S, 
         const uint32_t idx = b + lane;
         if (idx < n) {
             const float4 o = P.sh_o[idx], d = P.sh_d[idx];
-            if (!any_hit<true>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR])) {
+            if (!any_hit_ww<true, false>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR])) {
                 const int slot = __float_as_int(d.w);
                 const float4 c = P.sh_c[idx], r = P.rad[slot];
                 P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
