@@ -48,7 +48,7 @@ BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry
 # DRAM bytes (read + write) per closest-hit ray of k_trace, from one ncu
 # capture of a bounce-0 launch (profiles/k_trace_c2_first_bounce.md); the
 # roofline's `traffic` scales it to a full launch by rays per launch.
-TRACE_DRAM_BYTES_PER_RAY = 62.3
+TRACE_DRAM_BYTES_PER_RAY = 62.2
 
 
 def parse():
@@ -424,7 +424,7 @@ def main():
     roof["traffic"] = round(TRACE_DRAM_BYTES_PER_RAY * rays / max(1, trace_launches))
     roof["traffic_note"] = ("ncu DRAM bytes per ray of a bounce-0 k_trace launch (small case of the same scene) "
                             "x rays per launch")
-    # the whole path's algorithmic bytes as SURVEY 8(d) defines them:
+    # the whole path's algorithmic bytes, per path:
     # sum over rays (32 B per node, 36 B per triangle) + 240 B per shaded
     # vertex (hit attributes, material, path state, hit record) + 12 B film
     paths1 = max(1, cnt["paths"])
