@@ -149,7 +149,10 @@ int nr_scene_create(const nr_scene_desc* desc, nr_scene** out);
 /* Builds a scene from the reference's scene-description text: one OBJ path
  * per line with optional -p x y z, -s k, and forced materials
  * -m=light r g b | -m=ggx r g b alpha ior | -m=ggxr r g b alpha |
- * -m=glass r g b ior (src/scene/loader.cpp:26-108). */
+ * -m=glass r g b ior (src/scene/loader.cpp:26-108). MTL texture maps
+ * (map_Kd, map_Ks) may be PNG, JPEG (baseline or progressive), PFM or
+ * binary PPM; 8-bit images are linearised as Texture::load does
+ * (src/scene/texture.cpp:13-19). */
 int nr_scene_load(const char* scene_desc, nr_scene** out);
 
 int nr_scene_destroy(nr_scene* scene);
