@@ -239,7 +239,9 @@ __device__ __forceinline__ void emit_shadow(const PathState& P, const NrcCtx& C,
     }
 }
 
-template <bool NRC>
+// MT: the shading category when it is known at compile time (a material
+// type, or CAT_MISS), -1 for any
+template <bool NRC, int MT = -1>
 __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
                                           const NrcCtx& C) {
     float4 h = P.hit[slot];
@@ -249,7 +251,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     f3 dir = xyz(dir4);
     f3 T = xyz(thr);
     int tri = __float_as_int(h.w);
-    if (tri < 0) {
+    if (MT == CAT_MISS || (MT < 0 && tri < 0)) {
         if (S.env_tex >= 0) {
             float4 r = P.rad[slot];
             f3 e = env_lookup(S, dir);
@@ -268,7 +270,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     float w0 = 1.0f - b1 - b2;
     f3 normal = normalized(w0 * xyz(s0) + b1 * xyz(s1) + b2 * xyz(s2));
     f3 wo = -dir;
-    const int type = S.mats[mat].type;
+    const int type = MT >= 0 ? MT : S.mats[mat].type;
     if (type == NR_MAT_LIGHT) {  // emitter: Ke * light_fac (rendererptls.cpp:33-36)
         const nr_material& M = S.mats[mat];
         float4 r = P.rad[slot];
@@ -281,6 +283,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     // texture coordinates: t0 = (s0.w, s1.w), t1 = (s2.w, s3.x), t2 = (s3.y, s3.z)
     f3 uv = mk(w0 * s0.w + b1 * s2.w + b2 * s3.y, w0 * s1.w + b1 * s3.x + b2 * s3.z, 0.f);
     MatView M = load_mat(S, mat, uv);
+    if (MT >= 0) M.type = MT;  // the switch over material types folds to one case
     f3 o = xyz(P.ray_o[slot]);
     f3 hit_pos = o + dir * h.x;
     Stream rng;
@@ -400,28 +403,40 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
     P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, (uint32_t)(depth + 1) | flags | train_flag);
 }
 
-// Shades the bucketed queue: categories are contiguous, so each warp mostly
-// runs one material's code.
-// Shading asks for 8 resident 128-thread blocks per SM (64 registers, a
-// few spills) instead of the 5 its 94 registers allow: it waits on memory,
-// and the extra warps pay. 1M-triangle frame: 646.3 Mpaths/s uncapped,
-// 651.8 at 6, 657.4 at 8, 647.3 at 10, 629.7 at 12.
+// Shading: one kernel per shading category of the bucketed queue (the five
+// material types, emitters, misses), each compiled with its category fixed
+// so the material switch folds to one case and the kernel keeps only that
+// material's registers. All seven are launched per bounce; each strides
+// over its device-side count with at most 32 rounds of resident blocks.
+// Measured on the 1M-triangle frame (Mpaths/s): one kernel for all
+// categories 761.6, per category 771.3 (C3, mixed materials: 751.4 ->
+// 761.2); 8, 32 or 128 rounds of blocks 769.9, 771.3, (C3) 759.7.
+// Blocks per SM asked of the register allocator: 8 (64 registers). For the
+// single kernel before: 646.3 uncapped (94 registers), 651.8 at 6, 657.4
+// at 8, 647.3 at 10, 629.7 at 12; per category 6 gives 763.3 against 771.3.
 #ifndef NR_SHADE_MINB
 #define NR_SHADE_MINB 8
 #endif
+#ifndef NR_SHADE_ROUNDS
+#define NR_SHADE_ROUNDS 32
+#endif
+template <bool NRC, int MT>
+__global__ void __launch_bounds__(128, NR_SHADE_MINB) k_shade(PathState P, DeviceScene S, Policy pol, int capacity,
+                                                              NrcCtx C) {
+    const uint32_t n = P.counters[CNT_CAT + MT];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        shade_one<NRC, MT>(P, S, pol, P.sorted[(size_t)MT * capacity + i], C);
+}
 template <bool NRC>
-__global__ void __launch_bounds__(128, NR_SHADE_MINB) k_shade(PathState P, DeviceScene S, Policy pol, int capacity, NrcCtx C) {
-    uint32_t cnt[NUM_CAT], start[NUM_CAT];
-    uint32_t total = 0;
-#pragma unroll
-    for (int c = 0; c < NUM_CAT; ++c) { cnt[c] = P.counters[CNT_CAT + c]; start[c] = total; total += cnt[c]; }
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        int c = 0;
-#pragma unroll
-        for (int k = 1; k < NUM_CAT; ++k) if (i >= start[k]) c = k;
-        int slot = P.sorted[(size_t)c * capacity + (i - start[c])];
-        shade_one<NRC>(P, S, pol, slot, C);
-    }
+static void launch_shade(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int blocks,
+                         const NrcCtx& C, cudaStream_t st) {
+    k_shade<NRC, NR_MAT_LAMBERT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    k_shade<NRC, NR_MAT_GGXR><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    k_shade<NRC, NR_MAT_GGX><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    k_shade<NRC, NR_MAT_GLASS><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    k_shade<NRC, NR_MAT_BLINNPHONG><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    k_shade<NRC, NR_MAT_LIGHT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    k_shade<NRC, CAT_MISS><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
 }
 
 // ---------------------------------------------------------------- shadow rays
@@ -618,13 +633,14 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
         default: k_trace<true, true><<<g_trace_blocks, 128, 0, st>>>(P, S, capacity); break;
     }
     if (ev) cudaEventRecord(ev[1], st);
-    // k_shade strides over the device count; max_count (an upper bound of
-    // it) sizes the grid, one thread per path (capping the grid at 4 or 16
-    // resident rounds of blocks measured 693-695 against 704 Mpaths/s)
+    // the shading kernels stride over their device counts; max_count (an
+    // upper bound of their sum) and NR_SHADE_ROUNDS size the grids
     int shade_blocks = (max_count + 127) / 128;
     if (shade_blocks < 1) shade_blocks = 1;
-    if (nrc) k_shade<true><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, *nrc);
-    else k_shade<false><<<shade_blocks, 128, 0, st>>>(P, S, pol, capacity, NrcCtx{});
+    const int most = g_num_sms * NR_SHADE_MINB * NR_SHADE_ROUNDS;
+    if (shade_blocks > most) shade_blocks = most;
+    if (nrc) launch_shade<true>(P, S, pol, capacity, shade_blocks, *nrc, st);
+    else launch_shade<false>(P, S, pol, capacity, shade_blocks, NrcCtx{}, st);
     if (ev) cudaEventRecord(ev[2], st);
     float4* tb = (nrc && nrc->direct) ? nrc->t_before : nullptr;
     switch ((count ? 2 : 0) + pol.trav) {

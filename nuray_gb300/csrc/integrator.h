@@ -67,7 +67,9 @@ __device__ __forceinline__ void wave_path(const WaveDesc& W, uint64_t g, int img
 void launch_setup(int num_sms);
 void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
                    cudaStream_t st);
-// trace + sort, shade, shadow, advance. ev (optional) receives 4 events.
+// trace + sort, shade (one kernel per shading category), shadow, advance:
+// BOUNCE_LAUNCHES kernels. ev (optional) receives 4 events.
+constexpr int BOUNCE_LAUNCHES = 3 + NUM_CAT;
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc);
 // Query and training-record counts are read from C.counters on the device.
