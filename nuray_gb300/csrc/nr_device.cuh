@@ -430,7 +430,12 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
                 float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
                 ++nt;
                 float t, u, v;
-                if (FAST ? tri_test_fast(o, d, g0, g1, g2, lt, t, u, v) : tri_test(o, d, g0, g1, g2, lt, t, u, v)) {
+                // t < lt within the leaf, and t <= best_t (a tie with the best
+                // so far still decides by leaf order): the next float above
+                // best_t as the limit rejects farther hits before the exact
+                // quotients (770.9 -> 772.8 Mpaths/s)
+                const float cap = fminf(lt, __uint_as_float(__float_as_uint(best_t) + 1u));
+                if (FAST ? tri_test_fast(o, d, g0, g1, g2, cap, t, u, v) : tri_test(o, d, g0, g1, g2, cap, t, u, v)) {
                     lt = t; li = ti;
                 }
             }
