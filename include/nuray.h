@@ -246,7 +246,10 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * consecutive samples of a tile of 32 / tile_samples pixels, tile_samples
  * by default the largest power of two up to 32 dividing spp, when the tile
  * divides the image; else 1: 8x4 pixel tiles of one sample when imgw % 8 ==
- * 0 and imgh % 4 == 0; else or with 0: scanline order),
+ * 0 and imgh % 4 == 0; else or with 0: scanline order), live_sync (with
+ * maxdepth: the bounce after which the live path count is read back each
+ * bounce; -1, the default, 5 for waves of more than 2^22 paths and never
+ * for smaller ones),
  * envis=1 (ptnee only, no reference counterpart: one environment light
  * sample per light-sampling vertex besides the area-light sample, weighted
  * against BSDF-sampled misses by the balance heuristic; same expected image),
