@@ -645,7 +645,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             std::swap(P.queue_in, P.queue_out);
             S.bounces++;
             S.trace_launches++;
-            S.kernel_launches += nr::BOUNCE_LAUNCHES;
+            S.kernel_launches += nr::bounce_launches(cap);
             // With a depth limit the loop runs exactly maxdepth bounces; without
             // one the live count is read back to find the end of the wave.
             if (A.pol.maxdepth == 0 || (live_sync > 0 && bounce + 1 >= live_sync)) {
@@ -789,7 +789,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
             P.vis = rec ? rec_vis + (size_t)bounce * C : nullptr;
             nr::launch_bounce(P, s->dev, pol1, cap, live, st, nullptr, false, nullptr);
             std::swap(P.queue_in, P.queue_out);
-            launches += nr::BOUNCE_LAUNCHES;
+            launches += nr::bounce_launches(cap);
             if (!live_after(bounce, live)) break;
         }
         nr::launch_collect(s->ps, W, s->adj_L.as<float>(), A.spp, A.pol.imgw, st);

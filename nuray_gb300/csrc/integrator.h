@@ -67,9 +67,11 @@ __device__ __forceinline__ void wave_path(const WaveDesc& W, uint64_t g, int img
 void launch_setup(int num_sms);
 void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
                    cudaStream_t st);
-// trace + sort, shade (one kernel per shading category), shadow, advance:
-// BOUNCE_LAUNCHES kernels. ev (optional) receives 4 events.
-constexpr int BOUNCE_LAUNCHES = 3 + NUM_CAT;
+// trace + sort, shade (one kernel per shading category for waves above
+// 2^22 paths, else one for all), shadow, advance: bounce_launches(capacity)
+// kernels. ev (optional) receives 4 events.
+constexpr int SHADE_SPLIT_MIN = 1 << 22;
+inline int bounce_launches(int capacity) { return capacity > SHADE_SPLIT_MIN ? 3 + NUM_CAT : 4; }
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc);
 // Query and training-record counts are read from C.counters on the device.
