@@ -98,7 +98,8 @@ struct nr_nrc {
     float* xf = nullptr;  // FP32 staging of caller inputs
     float* loss_host = nullptr;  // pinned
     bool tc = true;              // inference on tcgen05 (nrc_tc.cu); false: mma.sync (nrc.cu)
-    DevBuf errbuf;               // error word of the tensor-core inference
+    DevBuf errbuf;               // error word of the tensor-core kernels
+    DevBuf wt_img;               // packed transposed weights of the tensor-core backward pass
     uint32_t* err_host = nullptr;  // pinned
 
     ~nr_nrc() {
@@ -109,6 +110,7 @@ struct nr_nrc {
         if (loss_host) cudaFreeHost(loss_host);
         if (err_host) cudaFreeHost(err_host);
         errbuf.release();
+        wt_img.release();
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -401,14 +403,30 @@ void nrc_ensure_batch(nr_nrc* c, int m) {
     c->batch_cap = m;
 }
 
+// Forward and backward of the rows R (gradients added to c->dev.grad, loss
+// to c->loss): on the tensor cores (tcgen05: forward and data gradients;
+// weight gradients by mma.sync) with tc, else all by mma.sync. err: the
+// word that receives bit 8 if a tensor-core wait timed out.
+void nrc_forward_backward(nr_nrc* c, const __nv_bfloat16* x, const float* y, const nr::NrcRows& R, uint32_t* err,
+                          cudaStream_t st) {
+    if (c->tc) {
+        nr::nrc_launch_forward_tc(c->dev.wb, c->dev.params, x, R, c->out, c->num_sms, err, st, c->acts);
+        nr::nrc_launch_backward_data_tc(c->dev.wb, c->out, y, c->acts, c->dz, R, c->loss, c->num_sms, c->wt_img.p, err,
+                                        st);
+        nr::nrc_launch_backward_weight(c->dev, x, c->dz, c->acts, R, c->num_sms, st);
+    } else {
+        nr::nrc_launch_forward(c->dev, x, R, c->out, c->acts, c->num_sms, st);
+        nr::nrc_launch_backward(c->dev, x, c->out, y, c->acts, c->dz, R, c->loss, c->num_sms, st);
+    }
+}
+
 // Gradient (and, when `update`, one Adam step) on m rows already on the
 // device: x BF16 [m][80], y [m][3]. Returns the summed loss asynchronously in c->loss.
 void nrc_train_device(nr_nrc* c, const __nv_bfloat16* x, const float* y, int m, bool update, cudaStream_t st) {
     nrc_ensure_batch(c, m);
     NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));
     const nr::NrcRows R = nr::nrc_rows(m);
-    nr::nrc_launch_forward(c->dev, x, R, c->out, c->acts, c->num_sms, st);
-    nr::nrc_launch_backward(c->dev, x, c->out, y, c->acts, c->dz, R, c->loss, c->num_sms, st);
+    nrc_forward_backward(c, x, y, R, c->errbuf.as<uint32_t>(), st);
     if (update) {
         c->step++;
         nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st);
@@ -675,8 +693,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             for (int k = 0; k < steps; ++k) {
                 const nr::NrcRows R = nr::nrc_rows_counted(&X.counters[1], s->nrc_tcap, k, steps);
                 const __nv_bfloat16* x = (const __nv_bfloat16*)X.t_x;
-                nr::nrc_launch_forward(c->dev, x, R, c->out, c->acts, c->num_sms, st);
-                nr::nrc_launch_backward(c->dev, x, c->out, c->y, c->acts, c->dz, R, c->loss, c->num_sms, st);
+                nrc_forward_backward(c, x, c->y, R, s->ps.counters + nr::CNT_ERR, st);
                 c->step++;
                 nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st);
             }
@@ -1194,6 +1211,7 @@ int nr_nrc_create(const char* params, nr_nrc** out) {
         nr::nrc_setup();
         nr::nrc_tc_setup();
         n->errbuf.alloc(256);
+        n->wt_img.alloc(nr::nrc_wt_image_bytes());
         NR_CUDA(cudaMemsetAsync(n->errbuf.p, 0, 4, n->stream));
         NR_CUDA(cudaMallocHost(&n->err_host, 4));
         const size_t P = NRC_NUM_PARAMS;
@@ -1306,8 +1324,10 @@ static int nrc_grad_impl(nr_nrc* c, int32_t n, const float* x, const float* y, f
             NR_CUDA(cudaMemsetAsync(c->dev.grad, 0, NRC_NUM_PARAMS * 4, c->stream));
         }
         NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, c->stream));
+        NR_CUDA(cudaMemcpyAsync(c->err_host, c->errbuf.p, 4, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaStreamSynchronize(c->stream));
         NR_CUDA(cudaGetLastError());
+        if (*c->err_host) throw NrError(NR_ERR_DEVICE, "tensor-core training wait timed out");
         if (loss) *loss = *c->loss_host;
     });
 }

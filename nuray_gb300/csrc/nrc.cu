@@ -453,6 +453,15 @@ void nrc_launch_backward(const NrcDev& N, const __nv_bfloat16* x, const float* o
     k_nrc_backward_weight<<<dim3(blocks, 5), 128, 0, st>>>(dz, x, acts, R, N.grad);
 }
 
+void nrc_launch_backward_weight(const NrcDev& N, const __nv_bfloat16* x, const __nv_bfloat16* dz,
+                                const __nv_bfloat16* acts, const NrcRows& R, int num_sms, cudaStream_t st) {
+    const int M = max_rows(R);
+    if (M <= 0) return;
+    int blocks = (M + 63) / 64;
+    if (blocks > num_sms * 2) blocks = num_sms * 2;
+    k_nrc_backward_weight<<<dim3(blocks, 5), 128, 0, st>>>(dz, x, acts, R, N.grad);
+}
+
 void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta,
                      const NrcRows& R, cudaStream_t st) {
     float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);

@@ -79,6 +79,18 @@ void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t
 // err (device word) gets bit 8 when a tensor-core wait timed out.
 void nrc_tc_setup();
 void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
-                           float* out, int num_sms, uint32_t* err, cudaStream_t st);
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts = nullptr);
+// Training on the tensor cores: the data gradients (dz [5][ld][64], loss)
+// of k_nrc_backward_data by tcgen05.mma; the weight gradients then come
+// from nrc_launch_backward_weight.
+// wt_img: nrc_wt_image_bytes() of device scratch for the packed transposed
+// weights.
+void nrc_launch_backward_data_tc(const __nv_bfloat16* wb, const float* out, const float* y, const __nv_bfloat16* acts,
+                                 __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms, void* wt_img,
+                                 uint32_t* err, cudaStream_t st);
+size_t nrc_wt_image_bytes();
+// The weight-gradient half of nrc_launch_backward (k_nrc_backward_weight).
+void nrc_launch_backward_weight(const NrcDev& N, const __nv_bfloat16* x, const __nv_bfloat16* dz,
+                                const __nv_bfloat16* acts, const NrcRows& R, int num_sms, cudaStream_t st);
 
 }  // namespace nr

@@ -111,12 +111,14 @@ __device__ void load_w(unsigned char* sm, int off, const __nv_bfloat16* __restri
 }  // namespace
 
 // Forward of the rows R over BF16 inputs [rows][80] with the BF16 weights
-// `wb` and the biases of `params`; out [rows][3] FP32. err bit 8 on a
-// tensor-core wait that timed out.
+// `wb` and the biases of `params`; out [rows][3] FP32; acts (may be null):
+// the hidden layers' post-ReLU BF16 activations [4][R.ld][64] for the
+// backward pass. err bit 8 on a tensor-core wait that timed out.
 __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __restrict__ wb,
                                                         const float* __restrict__ params,
                                                         const __nv_bfloat16* __restrict__ x, NrcRows R,
-                                                        float* __restrict__ out, uint32_t* err) {
+                                                        float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
+                                                        uint32_t* err) {
     int m0, M;
     if (!R.count) {
         m0 = 0;
@@ -131,6 +133,7 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
     if ((int)blockIdx.x >= tiles) return;  // the whole CTA: no tensor memory taken
     x += (size_t)m0 * IN;
     out += (size_t)m0 * 3;
+    const size_t LS = (size_t)R.ld * H;  // one layer of acts
 
     extern __shared__ __align__(1024) unsigned char sm[];
     float* sbias = reinterpret_cast<float*>(sm + SM_BIAS);
@@ -226,6 +229,8 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
                         pk.z = pack_bf16(fmaxf(v[8 * h2 + 4] + b[c0 + 4], 0.f), fmaxf(v[8 * h2 + 5] + b[c0 + 5], 0.f));
                         pk.w = pack_bf16(fmaxf(v[8 * h2 + 6] + b[c0 + 6], 0.f), fmaxf(v[8 * h2 + 7] + b[c0 + 7], 0.f));
                         *reinterpret_cast<uint4*>(dst + (c0 / 8) * 128) = pk;
+                        if (acts && row < M)
+                            *reinterpret_cast<uint4*>(acts + (size_t)layer * LS + (size_t)row * H + c0) = pk;
                     }
                 }
             } else {
@@ -249,20 +254,216 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
     }
 }
 
+// Data gradients on the tensor cores for the rows R: the relative L2
+// loss's gradient dOut (o - y) 2 / (o^2 + 0.01) / (3 rows), then per tile
+// of 128 rows the chain dA3 = dOut W4, dZ3 = dA3 (A3 > 0), dA2 = dZ3 W3, ...,
+// dZ0, each product one group of tcgen05.mma with the transposed weight
+// (B[n][k] = W[k][n]) in shared memory. dz [5][R.ld][64] BF16 as
+// k_nrc_backward_data writes it (layer 4: 8 columns), for
+// k_nrc_backward_weight; loss_sum (may be null) += the mean loss.
+namespace {
+constexpr int BK_W4T = 0;                                  // 64 x 16
+constexpr int BK_W3T = BK_W4T + (H / 8) * 2 * 128;         // 64 x 64 each
+constexpr int BK_W2T = BK_W3T + (H / 8) * KC_H * 128;
+constexpr int BK_W1T = BK_W2T + (H / 8) * KC_H * 128;
+constexpr int BK_A = BK_W1T + (H / 8) * KC_H * 128;        // 128 x 64 (the first product uses 128 x 16)
+constexpr int BK_BAR = BK_A + (TM / 8) * KC_H * 128;
+constexpr int BK_TOTAL = BK_BAR + 16;
+
+// W [k][n] (row-major, `n_in` columns, `k_real` rows, the rest zero) into
+// the canonical K-major layout of B[n][k] with K = kk, at dst + off.
+__device__ void load_wt(unsigned char* sm, int off, const __nv_bfloat16* __restrict__ w, int n_in, int k_real, int kk) {
+    const int kc = kk / 8;
+    // consecutive threads read consecutive elements of a row of W
+    for (int i = threadIdx.x; i < n_in * kk; i += blockDim.x) {
+        const int k = i / n_in, n = i % n_in;
+        const __nv_bfloat16 v = k < k_real ? w[(size_t)k * n_in + n] : __float2bfloat16(0.f);
+        *reinterpret_cast<__nv_bfloat16*>(sm + off + (n / 8) * (kc * 128) + (k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2) = v;
+    }
+}
+}  // namespace
+
+// The four transposed weight images of k_nrc_backward_data_tc (one per
+// block), packed once per pass into `img` (BK_A bytes) from which every CTA
+// copies them.
+__global__ void k_nrc_pack_wt(const __nv_bfloat16* __restrict__ wb, unsigned char* __restrict__ img) {
+    switch (blockIdx.x) {
+        case 0: load_wt(img, BK_W4T, wb + NRC_OFF_W4, H, NRC_OUT_PAD, 16); break;
+        case 1: load_wt(img, BK_W3T, wb + NRC_OFF_W3, H, H, H); break;
+        case 2: load_wt(img, BK_W2T, wb + NRC_OFF_W2, H, H, H); break;
+        default: load_wt(img, BK_W1T, wb + NRC_OFF_W1, H, H, H); break;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_nrc_backward_data_tc(const __nv_bfloat16* __restrict__ wb,
+                                                              const float* __restrict__ out,
+                                                              const float* __restrict__ y,
+                                                              const __nv_bfloat16* __restrict__ acts, NrcRows R,
+                                                              __nv_bfloat16* __restrict__ dz, float* loss_sum,
+                                                              const unsigned char* __restrict__ wt_img,
+                                                              uint32_t* err) {
+    int m0, M;
+    if (!R.count) {
+        m0 = 0;
+        M = R.n;
+    } else {
+        const int total = min((int)*R.count, R.n);
+        const int chunk = (total + R.steps - 1) / R.steps;
+        m0 = R.step * chunk;
+        M = max(0, min(chunk, total - m0));
+    }
+    const int tiles = (M + TM - 1) / TM;
+    if ((int)blockIdx.x >= tiles) return;
+    out += (size_t)m0 * 3;
+    y += (size_t)m0 * 3;
+    const size_t LS = (size_t)R.ld * H;
+    const float inv_n = 1.0f / (3.0f * (float)M);
+
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < BK_A / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(sm)[i] = reinterpret_cast<const uint4*>(wt_img)[i];
+    const uint32_t bar = smem_u32(sm + BK_BAR);
+    if (tid == 0) {
+        s_abort = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_taddr)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = s_taddr;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0;
+    const uint32_t a_addr = smem_u32(sm + BK_A);
+    const uint32_t wt_addr[4] = {smem_u32(sm + BK_W4T), smem_u32(sm + BK_W3T), smem_u32(sm + BK_W2T),
+                                 smem_u32(sm + BK_W1T)};
+    float loss = 0.f;
+
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int r = tid, row = tile * TM + r;
+        {  // dOut of this row -> A (K = 16) and dz[4]
+            float d[3] = {0.f, 0.f, 0.f};
+            if (row < M) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float o = out[(size_t)row * 3 + c], target = y[(size_t)row * 3 + c];
+                    const float den = o * o + 0.01f, diff = o - target;
+                    loss += diff * diff / den;
+                    d[c] = 2.f * diff / den * inv_n;
+                }
+            }
+            const uint4 pk = make_uint4(pack_bf16(d[0], d[1]), pack_bf16(d[2], 0.f), 0u, 0u);
+            unsigned char* dst = sm + BK_A + (r / 8) * (2 * 128) + (r % 8) * 16;
+            *reinterpret_cast<uint4*>(dst) = pk;
+            *reinterpret_cast<uint4*>(dst + 128) = make_uint4(0u, 0u, 0u, 0u);
+            if (row < M) *reinterpret_cast<uint4*>(dz + 4 * LS + (size_t)row * H) = pk;
+        }
+        // products with W4, W3, W2, W1; the epilogue of each gives dZ3, dZ2, dZ1, dZ0
+        for (int g = 0; g < 4; ++g) {
+            const int k = g == 0 ? 16 : H;
+            const uint32_t sbo = (uint32_t)(k / 8) * 128u;
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after();
+#pragma unroll 1
+                for (int ks = 0; ks < k / 16; ++ks) {
+                    const uint64_t ad = sdesc(a_addr + (uint32_t)ks * 256u, 128u, sbo);
+                    const uint64_t bd = sdesc(wt_addr[g] + (uint32_t)ks * 256u, 128u, sbo);
+                    mma(tmem, ad, bd, idesc_bf16((uint32_t)H), ks > 0 ? 1u : 0u);
+                }
+                commit(bar);
+            }
+            const bool ok = wait_phase(bar, phase);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(err, 8u);
+                    s_abort = 1;
+                }
+                break;
+            }
+            fence_after();
+            const int l = 3 - g;  // the layer whose dZ this epilogue forms
+            unsigned char* dst = sm + BK_A + (r / 8) * (KC_H * 128) + (r % 8) * 16;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float v[16];
+                tmem_ld16(lane_base + (uint32_t)(16 * q), v);
+#pragma unroll
+                for (int h2 = 0; h2 < 2; ++h2) {
+                    const int c0 = 16 * q + 8 * h2;
+                    uint4 av = make_uint4(0u, 0u, 0u, 0u);
+                    if (row < M) av = *reinterpret_cast<const uint4*>(acts + (size_t)l * LS + (size_t)row * H + c0);
+                    const uint32_t aw[4] = {av.x, av.y, av.z, av.w};
+                    uint32_t pw[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float lo = __uint_as_float(aw[e] << 16), hi = __uint_as_float(aw[e] & 0xffff0000u);
+                        pw[e] = pack_bf16(lo > 0.f ? v[8 * h2 + 2 * e] : 0.f, hi > 0.f ? v[8 * h2 + 2 * e + 1] : 0.f);
+                    }
+                    const uint4 pk = make_uint4(pw[0], pw[1], pw[2], pw[3]);
+                    *reinterpret_cast<uint4*>(dst + (c0 / 8) * 128) = pk;
+                    if (row < M) *reinterpret_cast<uint4*>(dz + (size_t)l * LS + (size_t)row * H + c0) = pk;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+    }
+    if (loss_sum) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+        if ((tid & 31) == 0) atomicAdd(loss_sum, loss * (1.0f / (3.0f * (float)M)));
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
 size_t nrc_forward_tc_smem() { return (size_t)SM_TOTAL; }
 
 void nrc_tc_setup() {
     cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc_forward_tc_smem());
+    cudaFuncSetAttribute(k_nrc_backward_data_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, BK_TOTAL);
 }
 
 void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
-                           float* out, int num_sms, uint32_t* err, cudaStream_t st) {
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts) {
     const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
     if (M <= 0) return;
     int blocks = (M + TM - 1) / TM;
     const int cap = num_sms * 3;  // three resident CTAs per SM by shared memory (64 tensor-memory columns each)
     if (blocks > cap) blocks = cap;
-    k_nrc_forward_tc<<<blocks, 128, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, err);
+    k_nrc_forward_tc<<<blocks, 128, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, acts, err);
+}
+
+size_t nrc_wt_image_bytes() { return (size_t)BK_A; }
+
+void nrc_launch_backward_data_tc(const __nv_bfloat16* wb, const float* out, const float* y, const __nv_bfloat16* acts,
+                                 __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms, void* wt_img,
+                                 uint32_t* err, cudaStream_t st) {
+    const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
+    if (M <= 0) return;
+    k_nrc_pack_wt<<<4, 256, 0, st>>>(wb, static_cast<unsigned char*>(wt_img));
+    int blocks = (M + TM - 1) / TM;
+    const int cap = num_sms * 4;  // 43 KB of shared memory and 64 tensor-memory columns per CTA
+    if (blocks > cap) blocks = cap;
+    k_nrc_backward_data_tc<<<blocks, 128, BK_TOTAL, st>>>(wb, out, y, acts, R, dz, loss_sum,
+                                                          static_cast<const unsigned char*>(wt_img), err);
 }
 
 }  // namespace nr

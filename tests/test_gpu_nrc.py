@@ -58,10 +58,13 @@ def test_forward_matches_torch(gpu_lib, tc):
     assert c.infer(x[:1]).shape == (1, 3)
 
 
-def test_gradient_matches_torch_and_finite_differences(gpu_lib):
+@pytest.mark.parametrize("tc", [1, 0])
+def test_gradient_matches_torch_and_finite_differences(gpu_lib, tc):
+    """tc=1: forward and data gradients by tcgen05.mma (nrc_tc.cu), weight
+    gradients by mma.sync; tc=0: all by mma.sync."""
     import torch
     from nuray_gb300.nrc import OFF, Cache, unpack
-    c = Cache("seed=5")
+    c = Cache(f"seed=5 tc={tc}")
     p = c.get_params()
     rng = np.random.default_rng(2)
     p = p + rng.normal(scale=0.02, size=p.size).astype(np.float32)
@@ -205,3 +208,27 @@ def test_tensor_core_forward_equals_mma_sync(gpu_lib):
         # rounding boundary can round the other way under the other order
         np.testing.assert_allclose(ya, yb, rtol=1e-2, atol=2e-3)
         assert np.mean(np.abs(ya - yb) <= 1e-5 + 1e-4 * np.abs(yb)) > 0.99
+
+
+def test_tensor_core_training_gradient_equals_mma_sync(gpu_lib):
+    """The same batch through both training paths: the gradients agree to
+    BF16 rounding of the activations and dZ (accumulation orders differ)."""
+    from nuray_gb300.nrc import OFF, Cache
+    rng = np.random.default_rng(12)
+    x = rand_inputs(5000, 9)  # several 128-row tiles and a ragged last one
+    y = rng.uniform(0, 2, size=(5000, 3)).astype(np.float32)
+    grads, losses = [], []
+    for tc in (1, 0):
+        c = Cache(f"seed=8 tc={tc}")
+        g, loss = c.gradient(x, y)
+        grads.append(g)
+        losses.append(loss)
+    assert abs(losses[0] - losses[1]) <= 1e-2 * abs(losses[1])
+    for k, (o, n) in OFF.items():
+        a, b = grads[0][o:o + n], grads[1][o:o + n]
+        if np.linalg.norm(b) < 1e-9:
+            assert np.linalg.norm(a) < 1e-6, k
+            continue
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
+        rel = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        assert cos > 0.999 and rel < 0.03, (k, cos, rel)
