@@ -323,6 +323,7 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
     float* gb = grad + boff;
     __shared__ __align__(16) __nv_bfloat16 sdz[64 * (H + 8)];
     __shared__ __align__(16) __nv_bfloat16 sx[64 * (IN + 8)];
+    __shared__ float sbias[64];
     const int SD = H + 8, SX = K + 8;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int n0 = 16 * warp;
@@ -331,19 +332,29 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
     float acc[10][4];
 #pragma unroll
     for (int j = 0; j < 10; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    // bias gradient: thread (column tid % 64, rows of half tid / 64) sums its
+    // column over the chunks, the halves meet in shared memory at the end
     float bsum = 0.f;
-    const __nv_bfloat16 z = __float2bfloat16(0.f);
+    const int bc = threadIdx.x & 63, bh = threadIdx.x >> 6;
+    if (threadIdx.x < 64) sbias[threadIdx.x] = 0.f;
     for (int m0 = blockIdx.x * 64; m0 < M; m0 += gridDim.x * 64) {
         __syncthreads();
-        for (int i = threadIdx.x; i < 64 * H; i += blockDim.x) {
-            int r = i / H, c = i % H;
-            sdz[r * SD + c] = (m0 + r < M && c < N) ? dz[(size_t)(m0 + r) * H + c] : z;
+        // 16-byte loads: rows of dZ (64 columns, those past N zero) and of X
+        for (int i = threadIdx.x; i < 64 * (H / 8); i += blockDim.x) {
+            const int r = i / (H / 8), c = 8 * (i % (H / 8));
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (m0 + r < M && c < N) v = *reinterpret_cast<const uint4*>(dz + (size_t)(m0 + r) * H + c);
+            *reinterpret_cast<uint4*>(&sdz[r * SD + c]) = v;
         }
-        for (int i = threadIdx.x; i < 64 * K; i += blockDim.x) {
-            int r = i / K, c = i % K;
-            sx[r * SX + c] = m0 + r < M ? xin[(size_t)(m0 + r) * K + c] : z;
+        for (int i = threadIdx.x; i < 64 * (K / 8); i += blockDim.x) {
+            const int r = i / (K / 8), c = 8 * (i % (K / 8));
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (m0 + r < M) v = *reinterpret_cast<const uint4*>(xin + (size_t)(m0 + r) * K + c);
+            *reinterpret_cast<uint4*>(&sx[r * SX + c]) = v;
         }
         __syncthreads();
+        if (bc < N)
+            for (int r = 32 * bh; r < 32 * bh + 32; ++r) bsum += bf(sdz[r * SD + bc]);
         if (!active) continue;
 #pragma unroll
         for (int ms = 0; ms < 4; ++ms) {
@@ -362,9 +373,10 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
                 mma16816(acc[jt], a, b0, b1);
             }
         }
-        if (lane < 16 && n0 + lane < N)
-            for (int r = 0; r < 64; ++r) bsum += bf(sdz[r * SD + n0 + lane]);
     }
+    if (bc < N) atomicAdd(&sbias[bc], bsum);
+    __syncthreads();
+    if (threadIdx.x < N) atomicAdd(&gb[threadIdx.x], sbias[threadIdx.x]);
     if (!active) return;
 #pragma unroll
     for (int jt = 0; jt < 10; ++jt) {
@@ -379,7 +391,6 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
             atomicAdd(&gW[(n0 + g + 8) * K + c + 1], acc[jt][3]);
         }
     }
-    if (lane < 16 && n0 + lane < N) atomicAdd(&gb[n0 + lane], bsum);
 }
 
 // Adam on the FP32 master parameters (Kingma & Ba), refreshing the BF16 copy
