@@ -149,3 +149,18 @@ def test_wavefront_replay_equals_one_thread_per_path(gpu_lib, case):
     np.testing.assert_array_equal(img_w, img_m)
     assert np.abs(gm).max() > 0
     np.testing.assert_allclose(gw, gm, rtol=1e-3, atol=1e-5 * np.abs(gm).max())
+
+
+def test_large_wave_adjoint_equals_split_waves(gpu_lib):
+    """A wave of more than 2^22 paths renders its first pass with one
+    shading kernel per category; the same samples in waves of 2^22 use one
+    kernel for all: same image, gradients equal to float rounding."""
+    sc = box_scene()
+    S = gpu(sc)
+    params = PARAMS.replace("spp=16", "spp=4096")  # 40 x 30 x 4096 = 4.9 M paths
+    W = loss_weights((30, 40, 3), 3)
+    g1, img1 = S.adjoint(params, W, want_image=True)
+    g2, img2 = S.adjoint(params + " wave=4194304", W, want_image=True)
+    np.testing.assert_allclose(img1, img2, rtol=1e-5, atol=1e-6)
+    assert np.abs(g1).max() > 0
+    np.testing.assert_allclose(g1, g2, rtol=1e-3, atol=1e-5 * np.abs(g1).max())

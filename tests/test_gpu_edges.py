@@ -132,3 +132,19 @@ def test_many_emitters_light_pick_matches_port(gpu_lib, port_lib):
     b = P.render_samples(sc["params"], pix, 4)
     assert np.all(np.isfinite(a)) and a.mean() > 0
     assert _sample_match(a, b) >= 0.97
+
+
+def test_category_shading_kernels_equal_the_single_kernel(gpu_lib):
+    """Waves of more than 2^22 paths shade with one kernel per shading
+    category (material type fixed at compile time), smaller ones with one
+    kernel for all categories: every material type, textures and an
+    environment, rendered as one wave of 6.3 M paths and as waves of 2^22."""
+    sc = scenes.small_scene(6, env=True, textures=True)
+    S = gpu_scene(sc)
+    p = sc["params"].replace("spp=4", "spp=4096")  # 48 x 32 x 4096 = 6.29 M paths
+    one = S.render(p)
+    split = S.render(p + " wave=4194304")
+    assert np.all(np.isfinite(one)) and one.mean() > 0
+    same = np.mean(one == split)
+    np.testing.assert_allclose(one, split, rtol=1e-5, atol=1e-6)
+    assert same >= 0.99, same
