@@ -249,7 +249,9 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * 0 and imgh % 4 == 0; else or with 0: scanline order), live_sync (with
  * maxdepth: the bounce after which the live path count is read back each
  * bounce; -1, the default, 5 for waves of more than 2^22 paths and never
- * for smaller ones),
+ * for smaller ones), tail (waves of at most 2^22 paths: after this many
+ * wavefront bounces one launch takes every live path to its end, tracing
+ * its light samples inline; default 2, 0 never; the image is the same),
  * envis=1 (ptnee only, no reference counterpart: one environment light
  * sample per light-sampling vertex besides the area-light sample, weighted
  * against BSDF-sampled misses by the balance heuristic; same expected image),

@@ -181,13 +181,17 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
         uint32_t idx = base + lane;
         if (idx < n) {
             float4 o = P.sh_o[idx], d = P.sh_d[idx];
+            const bool env = o.w < 0.f;  // an environment sample: k_env_fold adds it
+            const float tmax = env ? -o.w : o.w;
             const bool occluded =
-                (NR_WW & 6) ? any_hit_ww<FAST, (NR_WW & 2) != 0>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                (NR_WW & 6) ? any_hit_ww<FAST, (NR_WW & 2) != 0>(S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
                                          COUNT ? &nt : nullptr)
-                      : any_hit<FAST>(S, xyz(o), xyz(d), o.w, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                      : any_hit<FAST>(S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
                                       COUNT ? &nt : nullptr);
             if (P.vis) P.vis[__float_as_int(d.w)] = occluded ? 0 : 1;
-            if (!occluded) {
+            if (env) {
+                if (occluded) P.sh_c[idx].x = P.sh_c[idx].y = P.sh_c[idx].z = 0.f;
+            } else if (!occluded) {
                 int slot = __float_as_int(d.w);
                 float4 c = P.sh_c[idx];
                 float4 r = P.rad[slot];
@@ -207,6 +211,24 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
     }
 }
 
+// After k_shadow: every environment sample of the bounce adds its
+// contribution (zero if occluded) to its path, after the path's area-light
+// sample; one environment sample per path, so one writer per slot.
+__global__ void k_env_fold(PathState P, float4* t_before) {
+    const uint32_t n = min(P.counters[CNT_SHADOW], (uint32_t)P.sh_cap);
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        if (!(P.sh_o[idx].w < 0.f)) continue;
+        const int slot = __float_as_int(P.sh_d[idx].w);
+        const float4 c = P.sh_c[idx], r = P.rad[slot];
+        P.rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.f);
+        const int rec = __float_as_int(c.w);
+        if (t_before && rec >= 0) {
+            const float4 b = t_before[rec];
+            t_before[rec] = make_float4(b.x + c.x, b.y + c.y, b.z + c.z, 0.f);
+        }
+    }
+}
+
 // ---------------------------------------------------------------- shading
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
@@ -220,13 +242,25 @@ __device__ __forceinline__ bool nrc_is_training(uint32_t pixel, uint32_t sample,
 // Queues a shadow ray (or, when no hit can come before the limit, adds its
 // contribution at once). rec: the training record whose target leaves this
 // light sample out, or -1.
-template <bool NRC>
-__device__ __forceinline__ void emit_shadow(const PathState& P, const NrcCtx& C, int slot, int rec, f3 so, f3 d,
-                                            float tmax, f3 c) {
+// TAIL: trace the shadow ray here (the any-hit walk of k_shadow) instead of
+// queueing it. env: the vertex's environment sample, queued with its limit
+// negated: k_shadow leaves its contribution in the queue entry (zero when
+// occluded) and k_env_fold adds it after the area-light samples, so each
+// path's radiance has one writer at a time and the restatement's order.
+template <bool NRC, bool TAIL = false>
+__device__ __forceinline__ void emit_shadow(const PathState& P, const DeviceScene& S, const Policy& pol,
+                                            const NrcCtx& C, int slot, int rec, f3 so, f3 d, float tmax, f3 c,
+                                            bool env = false) {
+    if (TAIL && tmax > 0.f) {
+        const bool occluded = pol.trav ? any_hit_ww<true, (NR_WW & 2) != 0>(S, so, d, tmax, &P.counters[CNT_ERR])
+                                       : any_hit_ww<false, (NR_WW & 2) != 0>(S, so, d, tmax, &P.counters[CNT_ERR]);
+        if (occluded) return;
+        tmax = 0.f;  // unoccluded: added below
+    }
     if (tmax > 0.f) {
         int q = warp_append(true, &P.counters[CNT_SHADOW]);
         if (q >= P.sh_cap) { atomicOr(&P.counters[CNT_ERR], 4u); return; }
-        P.sh_o[q] = make_float4(so.x, so.y, so.z, tmax);
+        P.sh_o[q] = make_float4(so.x, so.y, so.z, env ? -tmax : tmax);
         P.sh_d[q] = make_float4(d.x, d.y, d.z, __int_as_float(slot));
         P.sh_c[q] = make_float4(c.x, c.y, c.z, __int_as_float(rec));
     } else {
@@ -240,9 +274,10 @@ __device__ __forceinline__ void emit_shadow(const PathState& P, const NrcCtx& C,
 }
 
 // MT: the shading category when it is known at compile time (a material
-// type, or CAT_MISS), -1 for any
-template <bool NRC, int MT = -1>
-__device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
+// type, or CAT_MISS), -1 for any. TAIL: light samples traced here and the
+// continuing path not queued. Returns whether the path goes on.
+template <bool NRC, int MT = -1, bool TAIL = false>
+__device__ __forceinline__ bool shade_one(const PathState& P, const DeviceScene& S, const Policy& pol, int slot,
                                           const NrcCtx& C) {
     float4 h = P.hit[slot];
     float4 thr = P.thr[slot];
@@ -260,7 +295,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
             if (dir4.w > 0.f && S.env_weight) e = e * (dir4.w / (dir4.w + env_pdf(S, dir)));
             P.rad[slot] = make_float4(r.x + T.x * e.x, r.y + T.y * e.y, r.z + T.z * e.z, 0.f);
         }
-        return;
+        return false;
     }
     float b1 = h.y, b2 = h.z;
     float4 s0 = __ldg(&S.tri_shade[4 * tri]), s1 = __ldg(&S.tri_shade[4 * tri + 1]);
@@ -276,10 +311,10 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
         float4 r = P.rad[slot];
         float lf = thr.w;
         P.rad[slot] = make_float4(r.x + T.x * M.c0[0] * lf, r.y + T.y * M.c0[1] * lf, r.z + T.z * M.c0[2] * lf, 0.f);
-        return;
+        return false;
     }
     // opaque back faces end the path (rendererptls.cpp:41-42)
-    if (dot(normal, dir) > 0.f && !mat_transmissive(type)) return;
+    if (dot(normal, dir) > 0.f && !mat_transmissive(type)) return false;
     // texture coordinates: t0 = (s0.w, s1.w), t1 = (s2.w, s3.x), t2 = (s3.y, s3.z)
     f3 uv = mk(w0 * s0.w + b1 * s2.w + b2 * s3.y, w0 * s1.w + b1 * s3.x + b2 * s3.z, 0.f);
     MatView M = load_mat(S, mat, uv);
@@ -308,7 +343,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
             C.q_thr[q] = make_float4(T.x, T.y, T.z, 0.f);
             nrc_encode(reinterpret_cast<uint32_t*>(C.q_x) + (size_t)q * 40, C.lo, C.inv_ext, hit_pos, wo, normal,
                        nrc_roughness(M), M.c0);
-            if (!C.direct) return;
+            if (!C.direct) return false;
             query_here = true;  // the light sample below stays explicit
         } else if (train) {
             int r = warp_append(true, &C.counters[1]);
@@ -359,7 +394,7 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
             // double there), i.e. occluded iff some hit has t <= |lv| - 2e-3.
             double lim = (double)norm(light_vec) - 2e-3;
             float tmax = lim > 0.0 ? __double2float_rd(lim) : 0.0f;
-            emit_shadow<NRC>(P, C, slot, rec, hit_pos + wl * 1e-3f, wl, tmax, c);
+            emit_shadow<NRC, TAIL>(P, S, pol, C, slot, rec, hit_pos + wl * 1e-3f, wl, tmax, c);
         }
     }
     // envis: one environment light sample more (no counterpart in the
@@ -379,28 +414,31 @@ __device__ __forceinline__ void shade_one(const PathState& P, const DeviceScene&
                 const float pb = last ? 0.f : mat_pdf(M, wo, normal, we);
                 const f3 c = T * mat_bxdf(M, wo, normal, we) * env_lookup(S, we) * (cosn / (pe + pb));
                 if (c.x != 0.f || c.y != 0.f || c.z != 0.f)
-                    emit_shadow<NRC>(P, C, slot, rec, hit_pos + we * 1e-3f, we, 3.0e38f, c);
+                    emit_shadow<NRC, TAIL>(P, S, pol, C, slot, rec, hit_pos + we * 1e-3f, we, 3.0e38f, c, true);
             }
         }
     }
-    if (NRC && query_here) return;
-    if (pol.maxdepth > 0 && depth + 1 >= pol.maxdepth) return;
+    if (NRC && query_here) return false;
+    if (pol.maxdepth > 0 && depth + 1 >= pol.maxdepth) return false;
     // Russian roulette (rendererptls.cpp:80-83)
     float prr = depth < pol.rrdepth ? 1.0f : pol.prr;
     float u = rng.next();
-    if (depth >= pol.rrdepth && (pol.excl ? !(u < prr) : u > prr)) return;  // renderernrc.cpp:162: go on while u < prr
+    if (depth >= pol.rrdepth && (pol.excl ? !(u < prr) : u > prr)) return false;  // renderernrc.cpp:162: go on while u < prr
     f3 wi = mat_sample(M, rng, wo, normal);
     float pdf = mat_pdf(M, wo, normal, wi);
     f3 brdf = mat_bxdf(M, wo, normal, wi);
     // contri = Li * |wi.n| * brdf / pdf / prr (rendererptls.cpp:90)
     f3 Tn = T * fabsf(dot(wi, normal)) * brdf / pdf / prr;
     f3 no = hit_pos + wi * 1e-3f;
-    int q = warp_append(true, &P.counters[CNT_OUT]);
-    P.queue_out[q] = slot;
+    if (!TAIL) {
+        int q = warp_append(true, &P.counters[CNT_OUT]);
+        P.queue_out[q] = slot;
+    }
     P.ray_o[slot] = make_float4(no.x, no.y, no.z, 0.f);
     P.ray_d[slot] = make_float4(wi.x, wi.y, wi.z, env_sampled ? pdf : 0.f);
     P.thr[slot] = make_float4(Tn.x, Tn.y, Tn.z, fac);
     P.meta[slot] = make_uint4(meta.x, meta.y, rng.n, (uint32_t)(depth + 1) | flags | train_flag);
+    return true;
 }
 
 // Shading: one kernel per shading category of the bucketed queue (the five
@@ -460,6 +498,30 @@ static void launch_shade(const PathState& P, const DeviceScene& S, const Policy&
     k_shade<NRC, NR_MAT_BLINNPHONG><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
     k_shade<NRC, NR_MAT_LIGHT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
     k_shade<NRC, CAT_MISS><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+}
+
+// The rest of every live path in one launch, one thread per path: closest
+// hit, then shade_one in its TAIL form (light samples traced inline), until
+// the path ends. For small waves, whose last bounces hold few rays: the
+// bounce-by-bounce wavefront waits at each bounce for its slowest ray, this
+// kernel only for the slowest path. Same functions, same results.
+#ifndef NR_TAIL_MAX_BOUNCES
+#define NR_TAIL_MAX_BOUNCES 4096
+#endif
+template <bool NRC, bool FAST>
+__global__ void __launch_bounds__(128, 4) k_tail(PathState P, DeviceScene S, Policy pol, NrcCtx C) {
+    const uint32_t n = P.counters[CNT_IN];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int slot = P.queue_in[i];
+    for (int b = 0; b < NR_TAIL_MAX_BOUNCES; ++b) {
+        const f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
+        float t, b1, b2;
+        const int tri = closest_hit_ww<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR]);
+        P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
+        if (!shade_one<NRC, -1, true>(P, S, pol, slot, C)) return;
+    }
+    atomicOr(&P.counters[CNT_ERR], 2u);  // step cap: the path did not end
 }
 
 // ---------------------------------------------------------------- shadow rays
@@ -646,6 +708,8 @@ void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, 
     k_raygen<<<(W.count + 255) / 256, 256, 0, st>>>(P, W, cam, film_h, pol);
 }
 
+static int count_grid(int cap);
+
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc) {
     if (ev) cudaEventRecord(ev[0], st);
@@ -672,8 +736,21 @@ void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, 
         case 2: k_shadow<true, false><<<g_shadow_blocks, 128, 0, st>>>(P, S, tb); break;
         default: k_shadow<true, true><<<g_shadow_blocks, 128, 0, st>>>(P, S, tb); break;
     }
+    if (pol.envis) k_env_fold<<<count_grid(P.sh_cap), 256, 0, st>>>(P, tb);
     if (ev) cudaEventRecord(ev[3], st);
     k_advance<<<1, 1, 0, st>>>(P.counters);
+}
+
+void launch_tail(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, const NrcCtx* nrc,
+                 cudaStream_t st) {
+    const int blocks = (capacity + 127) / 128;
+    if (nrc) {
+        if (pol.trav) k_tail<true, true><<<blocks, 128, 0, st>>>(P, S, pol, *nrc);
+        else k_tail<true, false><<<blocks, 128, 0, st>>>(P, S, pol, *nrc);
+    } else {
+        if (pol.trav) k_tail<false, true><<<blocks, 128, 0, st>>>(P, S, pol, NrcCtx{});
+        else k_tail<false, false><<<blocks, 128, 0, st>>>(P, S, pol, NrcCtx{});
+    }
 }
 
 void launch_trace(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, cudaStream_t st) {

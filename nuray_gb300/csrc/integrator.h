@@ -68,10 +68,13 @@ void launch_setup(int num_sms);
 void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
                    cudaStream_t st);
 // trace + sort, shade (one kernel per shading category for waves above
-// 2^22 paths, else one for all), shadow, advance: bounce_launches(capacity)
-// kernels. ev (optional) receives 4 events.
+// 2^22 paths, else one for all), shadow, (envis: the environment samples'
+// fold), advance: bounce_launches(capacity, envis) kernels. ev (optional)
+// receives 4 events.
 constexpr int SHADE_SPLIT_MIN = 1 << 22;
-inline int bounce_launches(int capacity) { return capacity > SHADE_SPLIT_MIN ? 3 + NUM_CAT : 4; }
+inline int bounce_launches(int capacity, bool envis) {
+    return (capacity > SHADE_SPLIT_MIN ? 3 + NUM_CAT : 4) + (envis ? 1 : 0);
+}
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc);
 // Query and training-record counts are read from C.counters on the device.
@@ -82,6 +85,10 @@ void launch_reset_counters(uint32_t* counters, cudaStream_t st);
 // that shade with kernels of their own (the adjoint replay).
 void launch_trace(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, cudaStream_t st);
 void launch_advance(uint32_t* counters, cudaStream_t st);
+// Every live path of queue_in to its end in one launch (after some
+// wavefront bounces of a small wave); capacity bounds the live count.
+void launch_tail(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, const NrcCtx* nrc,
+                 cudaStream_t st);
 // k_trace's sort by shading category for hits recorded in P.hit by an earlier pass
 void launch_sort_recorded(const PathState& P, const DeviceScene& S, int capacity, cudaStream_t st);
 int shadow_grid();  // blocks of the persistent shadow-ray kernels
