@@ -311,7 +311,7 @@ int nr_nrc_gradient(nr_nrc* nrc, int32_t n, const float* x, const float* y, floa
 int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, float* loss);
 /* Attaches a cache to a scene: nr_render with nrc=1 then ends non-training
  * paths at the vertex after their first diffuse bounce (a Lambert or
- * BlinnPhong vertex, or GGX with roughness >= nrc_rough, default 0.2), at
+ * BlinnPhong vertex, or GGX with roughness >= nrc_rough, default 0.05), at
  * vertex depth >= nrc_mindepth (default 1), with the cache's prediction, and
  * trains the cache online on the suffix radiance of nrc_train (default
  * 16384) training paths per wavefront batch in nrc_steps (default 2) Adam

@@ -532,7 +532,10 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.nrc_steps = c.get_int("nrc_steps", 2);
     a.nrc_query = c.get_int("nrc_query", 1);
     a.nrc_mindepth = nrc_mode ? c.get_int("path_lim", 2) : c.get_int("nrc_mindepth", 1);
-    a.nrc_rough = c.get_float("nrc_rough", 0.2f);
+    // GGX vertices from this roughness on count as diffuse for ending paths
+    // in the cache. Time to relMSE 1e-3 at 960x540, 64 spp per frame: 2.78 s
+    // at 0.2, 2.72 at 0.1, 2.69 at 0.05 and at 0 (plain PT 2.89).
+    a.nrc_rough = c.get_float("nrc_rough", 0.05f);
     a.nrc_direct = nrc_mode ? 0 : (c.get_int("nrc_direct", 1) != 0 ? 1 : 0);
     a.nrc_train_depth = nrc_mode ? c.get_int("path_lim_train", 4) : c.get_int("nrc_train_depth", 3);
     if (a.nrc_train_depth < 0) throw NrError(NR_ERR_INVALID, "nrc_train_depth must be >= 0");
