@@ -96,6 +96,23 @@ def test_intersect_million_triangles(gpu_lib, port_lib):
     assert info["tris"] == sc["pos"].shape[0] and info["depth"] < 96
 
 
+def test_samples_million_triangles_vs_port(gpu_lib, port_lib):
+    """The benchmark frame's own scene and parameters (1M triangles, 32 quad
+    lights, GGX-reflect materials, 1920x1080, maxdepth 8, RR from 3): the
+    per-sample radiance of a spread of pixels on the shared Philox stream,
+    GPU against the CPU restatement (a wave this small finishes its paths in
+    the tail kernel after two bounces)."""
+    sc = scenes.terrain_spheres(0)
+    S = gpu_scene(sc)
+    P = Oracle("port", sc)
+    rng = np.random.default_rng(21)
+    pix = np.stack([rng.integers(0, 1920, 400), rng.integers(0, 1080, 400)], 1).astype(np.int32)
+    a = S.render_samples(sc["params"], pix, 4)
+    b = P.render_samples(sc["params"], pix, 4)
+    assert np.all(np.isfinite(a)) and a.mean() > 0
+    assert _sample_match(a, b) >= 0.97
+
+
 def test_material_probes(gpu_lib):
     g = golden("small_ref.npz")
     sc = scenes.small_scene()
