@@ -314,6 +314,9 @@ void upload_scene(nr_scene* s) {
     D.light_p = (float)(1.0 / ((double)sum + 1e-8));
     D.num_tris = n;
     D.num_mats = (int)H.mats.size();
+    D.cat_mask = 1u << nr::CAT_MISS;
+    for (const auto& m : H.mats)
+        if (m.type >= 0 && m.type < nr::CAT_MISS) D.cat_mask |= 1u << m.type;
     D.env_tex = H.env_tex;
     D.env_gain = H.env_gain;
     D.max_depth = B.max_depth;
@@ -678,7 +681,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             std::swap(P.queue_in, P.queue_out);
             S.bounces++;
             S.trace_launches++;
-            S.kernel_launches += nr::bounce_launches(cap, A.pol.envis != 0);
+            S.kernel_launches += nr::bounce_launches(cap, A.pol.envis != 0, s->dev.cat_mask);
             // With a depth limit the loop runs exactly maxdepth bounces; without
             // one the live count is read back to find the end of the wave.
             if (A.pol.maxdepth == 0 || (live_sync > 0 && bounce + 1 >= live_sync)) {
@@ -821,7 +824,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
             P.vis = rec ? rec_vis + (size_t)bounce * C : nullptr;
             nr::launch_bounce(P, s->dev, pol1, cap, live, st, nullptr, false, nullptr);
             std::swap(P.queue_in, P.queue_out);
-            launches += nr::bounce_launches(cap, false);
+            launches += nr::bounce_launches(cap, false, s->dev.cat_mask);
             if (!live_after(bounce, live)) break;
         }
         nr::launch_collect(s->ps, W, s->adj_L.as<float>(), A.spp, A.pol.imgw, st);

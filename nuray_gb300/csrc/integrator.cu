@@ -491,12 +491,14 @@ static void launch_shade(const PathState& P, const DeviceScene& S, const Policy&
         k_shade<NRC, -1><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
         return;
     }
-    k_shade<NRC, NR_MAT_LAMBERT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
-    k_shade<NRC, NR_MAT_GGXR><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
-    k_shade<NRC, NR_MAT_GGX><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
-    k_shade<NRC, NR_MAT_GLASS><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
-    k_shade<NRC, NR_MAT_BLINNPHONG><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
-    k_shade<NRC, NR_MAT_LIGHT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    // categories of material types absent from the scene can hold no path
+    if (S.cat_mask & (1u << NR_MAT_LAMBERT)) k_shade<NRC, NR_MAT_LAMBERT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    if (S.cat_mask & (1u << NR_MAT_GGXR)) k_shade<NRC, NR_MAT_GGXR><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    if (S.cat_mask & (1u << NR_MAT_GGX)) k_shade<NRC, NR_MAT_GGX><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    if (S.cat_mask & (1u << NR_MAT_GLASS)) k_shade<NRC, NR_MAT_GLASS><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    if (S.cat_mask & (1u << NR_MAT_BLINNPHONG))
+        k_shade<NRC, NR_MAT_BLINNPHONG><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
+    if (S.cat_mask & (1u << NR_MAT_LIGHT)) k_shade<NRC, NR_MAT_LIGHT><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
     k_shade<NRC, CAT_MISS><<<blocks, 128, 0, st>>>(P, S, pol, capacity, C);
 }
 

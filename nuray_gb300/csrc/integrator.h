@@ -67,13 +67,13 @@ __device__ __forceinline__ void wave_path(const WaveDesc& W, uint64_t g, int img
 void launch_setup(int num_sms);
 void launch_raygen(const PathState& P, const WaveDesc& W, const nr_camera& cam, float film_h, const Policy& pol,
                    cudaStream_t st);
-// trace + sort, shade (one kernel per shading category for waves above
-// 2^22 paths, else one for all), shadow, (envis: the environment samples'
-// fold), advance: bounce_launches(capacity, envis) kernels. ev (optional)
-// receives 4 events.
+// trace + sort, shade (for waves above 2^22 paths one kernel per shading
+// category the scene's materials can produce, else one for all), shadow,
+// (envis: the environment samples' fold), advance: bounce_launches(capacity,
+// envis, scene category mask) kernels. ev (optional) receives 4 events.
 constexpr int SHADE_SPLIT_MIN = 1 << 22;
-inline int bounce_launches(int capacity, bool envis) {
-    return (capacity > SHADE_SPLIT_MIN ? 3 + NUM_CAT : 4) + (envis ? 1 : 0);
+inline int bounce_launches(int capacity, bool envis, uint32_t cat_mask) {
+    return (capacity > SHADE_SPLIT_MIN ? 3 + __builtin_popcount(cat_mask) : 4) + (envis ? 1 : 0);
 }
 void launch_bounce(const PathState& P, const DeviceScene& S, const Policy& pol, int capacity, int max_count,
                    cudaStream_t st, cudaEvent_t* ev, bool count, const NrcCtx* nrc);

@@ -58,6 +58,7 @@ struct DeviceScene {
     const float* env_row_cdf;
     const float* env_col_cdf;
     float env_total;
+    uint32_t cat_mask;        // shading categories that can occur: bit t for each material type present, and misses
     int32_t max_depth;        // deepest leaf (root = 0)
     int32_t num_nodes;        // internal nodes
 };
