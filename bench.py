@@ -100,12 +100,15 @@ def workload(args):
     params = params.replace("spp=64", f"spp={args.spp}").replace("spp=256", f"spp={args.spp}")
     if args.wave:
         params += f" wave={args.wave}"
+    if args.workload == "c3":
+        params += " envis=1"  # the environment map's importance sampling (IBL) the workload names
     if args.params:
         params += " " + args.params
     desc = (f"procedural terrain+spheres, {sc['pos'].shape[0]} triangles, {w}x{h}, spp={args.spp}, "
             "maxdepth 8, RR from depth 3, GGX-reflect materials, 32 quad lights, Philox seed 0")
     if args.workload == "c3":
-        desc += ", 2048x1024 HDR sky (peak 5e3), 512x512 value-noise textures on half the materials, 10% GGX dielectrics"
+        desc += (", 2048x1024 HDR sky (peak 5e3) with environment importance sampling (envis=1), 512x512 "
+                 "value-noise textures on half the materials, 10% GGX dielectrics")
     return sc, params, desc, w, h
 
 
