@@ -1,6 +1,10 @@
-// Cache inference on the 5th-generation tensor cores: the 80-64-64-64-64-3
-// MLP of nrc.cu as a chain of tcgen05.mma (kind::f16, BF16 operands, FP32
-// accumulators in tensor memory), 128 rows per CTA tile.
+// The cache's MLP on the 5th-generation tensor cores: the 80-64-64-64-64-3
+// network of nrc.cu as chains of tcgen05.mma (kind::f16, BF16 operands,
+// FP32 accumulators in tensor memory), 128 rows per CTA tile. The forward
+// kernel serves inference and, storing the hidden activations, training;
+// the data-gradient kernel runs the same chain backwards against the
+// transposed weights (its own comment below). Weight gradients and Adam
+// stay in nrc.cu.
 //
 // Per tile: the 128 input rows go to shared memory in the canonical K-major
 // layout without swizzle (8-row x 16-byte core matrices; the leading byte
