@@ -1004,6 +1004,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         if (A.adj_mega) {
             RenderArgs P1 = A;
             P1.tile = 0;
+            P1.tail = 0;  // the wavefront to the end, as the wavefront adjoint's first pass
             run_waves(s, P1, npix, nullptr, A.sample0, nullptr, s->adj_L.as<float>(), nullptr, nullptr, nullptr);
             nr::launch_adjoint(J, d_dldi, d_grad, s->adj_L.as<float>(), s->num_sms, st);
             launches = s->stats.kernel_launches + 1;
