@@ -569,6 +569,11 @@ void wave_layout(const RenderArgs& A, bool has_pix_list, nr::WaveDesc& W) {
     else if (A.tile >= 1 && A.pol.imgw % 8 == 0 && A.pol.imgh % 4 == 0) W.tiled = 1;
 }
 
+// Bound on the bounces of a wave without a depth limit (the tail kernel's
+// NR_TAIL_MAX_BOUNCES too): paths end by Russian roulette, misses and
+// emitters, but prr = 1 in a closed scene would never end.
+constexpr int kMaxBounces = 4096;
+
 void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pix, int sample0, float4* film,
                float* dev_out, volatile int32_t* cancel, void (*progress)(float, void*), void* user) {
     const uint64_t total = (uint64_t)npix * (uint64_t)A.spp;
@@ -660,6 +665,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         const bool tail = A.tail > 0 && cap <= nr::SHADE_SPLIT_MIN && !A.profile && !A.count;
         for (int bounce = 0;; ++bounce) {
             if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
+            if (bounce >= kMaxBounces) throw NrError(NR_ERR_DEVICE, "paths still alive after 4096 bounces (prr = 1?)");
             if (tail && bounce >= A.tail) {
                 nr::launch_tail(P, s->dev, A.pol, cap, use_nrc ? &s->nrc_ctx : nullptr, st);
                 S.kernel_launches += 1;
@@ -819,6 +825,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
         int live = W.count;
         for (int bounce = 0;; ++bounce) {
             if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
+            if (bounce >= kMaxBounces) throw NrError(NR_ERR_DEVICE, "paths still alive after 4096 bounces (prr = 1?)");
             const bool rec = bounce < depth_rec;
             P.hit = rec ? rec_hit + (size_t)bounce * C : s->ps.hit;
             P.vis = rec ? rec_vis + (size_t)bounce * C : nullptr;
@@ -837,6 +844,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
         live = W.count;
         for (int bounce = 0;; ++bounce) {
             if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
+            if (bounce >= kMaxBounces) throw NrError(NR_ERR_DEVICE, "paths still alive after 4096 bounces (prr = 1?)");
             const bool rec = bounce < depth_rec;
             const uint8_t* vis = nullptr;
             if (rec) {

@@ -170,3 +170,26 @@ def test_tail_kernel_gives_the_same_image(gpu_lib, envis):
     a, b = c.render(q + " tail=2"), c.render(q)
     np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-7)
     assert np.mean(a == b) >= 0.999
+
+
+def closed_cube(half=100.0):
+    """Inward-facing cube of 12 triangles, white diffuse, no emitter."""
+    v = np.array([[x, y, z] for x in (-half, half) for y in (-half, half) for z in (-half, half)], np.float32)
+    quads = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    tris = [t for a, b, c, d in quads for t in ((a, c, b), (a, d, c))]  # quads wind outward: reversed
+    pos = np.stack([v[list(t)].reshape(9) for t in tris]).astype(np.float32)
+    return pos
+
+
+@pytest.mark.parametrize("tail", [0, 2])
+def test_endless_paths_stop_with_an_error(gpu_lib, tail):
+    """prr=1 without a depth limit inside a closed white box: no path ever
+    ends (the reference would loop forever). The render stops after 4096
+    bounces with an error instead, and the scene stays usable."""
+    from nuray_gb300 import NuRayError, Scene
+    S = Scene.from_arrays(closed_cube(), np.zeros(12, np.int32), [dict(type=0, c0=[1, 1, 1])])
+    p = "renderer=ptnee imgw=8 imgh=8 spp=16 campos=0,0,0 cameuler=0,0,0 camfov=64 camasp=1"
+    with pytest.raises(NuRayError, match="4096 bounces|error bits 2"):
+        S.render(p + f" prr=1 maxdepth=0 tail={tail}")
+    img = S.render(p + f" tail={tail}")  # default prr: paths end, no light: black
+    assert np.all(img == 0)
