@@ -109,6 +109,9 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // the shadow queue sorted by light (counting sort, 257 buckets) before the
 // shadow kernel, 541: rays from neighbouring pixels to different lights
 // share more of their walk than rays to one light from across the frame.
+// Likewise within a warp's window of 128 or 256 queued rays, grouped by the
+// cell of a 4x4x4 grid holding the ray's end point (counting sort in shared
+// memory): 756.1 and 743.3 against 772.1.
 #ifndef NR_TRACE_MINB
 #define NR_TRACE_MINB 10
 #endif
