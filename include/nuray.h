@@ -47,7 +47,8 @@ extern "C" {
 #define NR_ERR_OOM (-3)        /* device or host allocation failed */
 #define NR_ERR_CANCELLED (-4)  /* *cancel became 0 during nr_render */
 #define NR_ERR_IO (-5)         /* a scene file could not be read */
-#define NR_ERR_DEVICE (-6)     /* a kernel reported an internal error (stack overflow, bad index) */
+#define NR_ERR_DEVICE (-6)     /* a kernel reported an internal error (stack overflow, bad index),
+                                  or paths still alive after 4096 bounces (prr=1, no maxdepth) */
 
 /* Material types: the reference's Material subclasses (src/material/). */
 #define NR_MAT_LAMBERT 0     /* MatLambert    (src/material/matlambert.cpp) */
