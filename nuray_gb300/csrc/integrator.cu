@@ -454,7 +454,9 @@ __device__ __forceinline__ bool shade_one(const PathState& P, const DeviceScene&
 // 761.2); 8, 32 or 128 rounds of blocks 769.9, 771.3, (C3) 759.7.
 // Blocks per SM asked of the register allocator: 8 (64 registers). For the
 // single kernel before: 646.3 uncapped (94 registers), 651.8 at 6, 657.4
-// at 8, 647.3 at 10, 629.7 at 12; per category 6 gives 763.3 against 771.3.
+// at 8, 647.3 at 10, 629.7 at 12; per category 6 gives 763.3 against 771.3;
+// re-checked with the tail kernel and the category mask: 6 / 8 / 10 give
+// 766.0 / 773.9 / 768.6.
 #ifndef NR_SHADE_MINB
 #define NR_SHADE_MINB 8
 #endif
