@@ -207,14 +207,17 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
                 commit(bar);
             }
             const bool ok = wait_phase(bar, phase);
-            phase ^= 1u;
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
                     atomicOr(err, 8u);
                     s_abort = 1;
+                    // the MMAs may still write the tensor memory freed below:
+                    // one more bounded wait for their commit
+                    wait_phase(bar, phase);
                 }
                 break;
             }
+            phase ^= 1u;
             fence_after();
             const int r = tid, row = tile * TM + r;
             if (layer < 4) {
@@ -389,14 +392,17 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data_tc(const __nv_bfloat1
                 commit(bar);
             }
             const bool ok = wait_phase(bar, phase);
-            phase ^= 1u;
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
                     atomicOr(err, 8u);
                     s_abort = 1;
+                    // the MMAs may still write the tensor memory freed below:
+                    // one more bounded wait for their commit
+                    wait_phase(bar, phase);
                 }
                 break;
             }
+            phase ^= 1u;
             fence_after();
             const int l = 3 - g;  // the layer whose dZ this epilogue forms
             unsigned char* dst = sm + BK_A + (r / 8) * (KC_H * 128) + (r % 8) * 16;
