@@ -179,3 +179,12 @@ def test_scene_export_renders_identically_in_the_reference(port_lib, ref_lib, tm
     a, b = P.render_samples(params, pix, 2, seed=1), R.render_samples(params, pix, 2, seed=1)
     assert a.mean() > 0
     np.testing.assert_array_equal(a, b)
+
+
+def test_scene_export_command(tmp_path, capsys):
+    scenes.main([str(tmp_path / "s"), "--small", "--seed", "2"])
+    out = capsys.readouterr().out
+    assert "triangles" in out
+    desc = (tmp_path / "s" / "scene.desc").read_text().splitlines()
+    assert desc and all(line.split()[0].endswith(".obj") for line in desc)
+    assert "renderer=ptnee" in (tmp_path / "s" / "scene.params").read_text()
