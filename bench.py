@@ -49,6 +49,10 @@ BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry
 # capture of a bounce-0 launch (profiles/k_trace_c2_first_bounce.md); the
 # roofline's `traffic` scales it to a full launch by rays per launch.
 TRACE_DRAM_BYTES_PER_RAY = 62.2
+# cache hit rates of the same capture (lts__t_sector_hit_rate,
+# l1tex__t_sector_hit_rate), reported beside the roofline
+TRACE_L2_HIT_RATE = 0.675
+TRACE_L1_HIT_RATE = 0.796
 
 
 def parse():
@@ -427,6 +431,9 @@ def main():
     roof["traffic"] = round(TRACE_DRAM_BYTES_PER_RAY * rays / max(1, trace_launches))
     roof["traffic_note"] = ("ncu DRAM bytes per ray of a bounce-0 k_trace launch (small case of the same scene) "
                             "x rays per launch")
+    roof["l2_hit_rate"] = TRACE_L2_HIT_RATE
+    roof["l1_hit_rate"] = TRACE_L1_HIT_RATE
+    roof["hit_rate_note"] = "ncu sector hit rates of the same bounce-0 k_trace capture"
     # the whole path's algorithmic bytes, per path:
     # sum over rays (32 B per node, 36 B per triangle) + 240 B per shaded
     # vertex (hit attributes, material, path state, hit record) + 12 B film
