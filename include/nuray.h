@@ -255,7 +255,9 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * its light samples inline; default 2, 0 never; the image is the same),
  * envis=1 (ptnee only, no reference counterpart: one environment light
  * sample per light-sampling vertex besides the area-light sample, weighted
- * against BSDF-sampled misses by the balance heuristic; same expected image),
+ * against BSDF-sampled misses by the balance heuristic; the same expected
+ * image where a material's pdf() is its sampling density, as for Lambert, but
+ * not on GGX-reflect, whose pdf() omits the half-vector Jacobian),
  * profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
  * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
  * (W*H*3 bytes: mean^(1/2.2)*255 clamped and truncated, as
