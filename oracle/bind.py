@@ -37,12 +37,48 @@ def build_port():
     return PORT_LIB
 
 
-def build_ref(ref_root="/root/reference"):
-    """Compiles the reference sources; returns the library path or None."""
+# Where the reference checkout lies (only the fixture script, the tests that
+# pin the oracle and build() read it; the GPU host has none).
+REF_ROOT = os.environ.get("NURAY_REF_ROOT", "/root/reference")
+REF_RENDER_LIB = os.path.join(HERE, "_ref", "libnuray_ref_render.so")
+
+
+def build_ref(ref_root=None):
+    """Compiles the reference sources (both oracle libraries); returns the
+    library path or None."""
+    ref_root = ref_root or REF_ROOT
     if not os.path.isdir(os.path.join(ref_root, "src", "renderer")):
         return None
-    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "ref-render", f"REF={ref_root}"], check=True)
     return REF_LIB
+
+
+def ref_render_image(scene, params, seed=0):
+    """The reference's RendererPTLS::render of the whole frame, 8-bit RGB
+    (h, w, 3), on the Philox stream (oracle/ref_render.cpp)."""
+    L = ctypes.CDLL(REF_RENDER_LIB)
+    L.ref_scene_from_arrays.restype = _vp
+    L.ref_scene_from_arrays.argtypes = _SIG["scene_create"][0][:13]
+    L.ref_scene_destroy.argtypes = [_vp]
+    L.ref_render_image.argtypes = [_vp, _cp, _u64, _vp]
+    L.ref_render_image.restype = _i32
+    pos = np.ascontiguousarray(scene["pos"], np.float32)
+    n = pos.shape[0]
+    uv = np.ascontiguousarray(scene.get("uv") if scene.get("uv") is not None else np.zeros((n, 6)), np.float32)
+    nrm = np.ascontiguousarray(scene.get("nrm") if scene.get("nrm") is not None else np.zeros((n, 9)), np.float32)
+    mat = np.ascontiguousarray(scene["mat"], np.int32)
+    mi, mf = _mat_arrays(scene["mats"])
+    h = L.ref_scene_from_arrays(n, _ptr(pos), _ptr(uv), _ptr(nrm), _ptr(mat), len(scene["mats"]), _ptr(mi), _ptr(mf),
+                                0, None, None, -1, 1.0)
+    cfg = dict(kv.split("=", 1) for kv in params.split() if "=" in kv)
+    w, hh = int(cfg.get("imgw", 1)), int(cfg.get("imgh", 1))
+    out = np.zeros((hh, w, 3), np.uint8)
+    try:
+        if L.ref_render_image(h, params.encode(), seed, _ptr(out)) != 0:
+            raise RuntimeError("the reference's render() did not finish")
+    finally:
+        L.ref_scene_destroy(h)
+    return out
 
 
 def _ptr(a):
@@ -115,6 +151,17 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+    def set_materials(self, mats):
+        """Port only: new material parameters (same count and types), the
+        BVH and the emitter table kept."""
+        if self.kind != "port":
+            raise ValueError("set_materials is a port entry point")
+        mi, mf = _mat_arrays(mats)
+        f = self.L.port_scene_set_materials
+        f.argtypes, f.restype = [_vp, _i32, _vp, _vp], _i32
+        if f(self.h, len(mats), _ptr(mi), _ptr(mf)) != 0:
+            raise ValueError("material count or types differ from the scene's")
 
     def bvh(self):
         f = getattr(self.L, self.pre + "bvh_export")

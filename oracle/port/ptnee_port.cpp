@@ -828,6 +828,25 @@ void* port_scene_create(int ntri, const float* pos, const float* uv, const float
 
 void port_scene_destroy(void* s) { delete static_cast<Scene*>(s); }
 
+// Replaces the material parameters (same count, same types) without
+// rebuilding the BVH; for finite differences over material parameters. The
+// emitter table depends only on the geometry and the types (radiance is
+// read from the materials where it is used), so it stays. Returns 0, or -1
+// on a count or type change.
+int port_scene_set_materials(void* s, int nmat, const int* mat_i, const float* mat_f) {
+    auto* S = static_cast<Scene*>(s);
+    if (nmat != (int)S->mats.size()) return -1;
+    for (int m = 0; m < nmat; ++m)
+        if (mat_i[4 * m] != S->mats[m].type) return -1;
+    for (int m = 0; m < nmat; ++m) {
+        Mat& M = S->mats[m];
+        const float* F = mat_f + 12 * m;
+        M.c0 = V3(F[0], F[1], F[2]); M.c1 = V3(F[3], F[4], F[5]);
+        M.alpha = F[6]; M.ior = F[7]; M.ns = F[8];
+    }
+    return 0;
+}
+
 int port_bvh_export(void* s, float* box, int* kids, int* leaf_first, int* leaf_count, int* leaf_tris, int* n_leaf_tris) {
     auto* S = static_cast<Scene*>(s);
     int nn = 0, nt = 0;

@@ -29,6 +29,7 @@ void* port_scene_create(int ntri, const float* pos, const float* uv, const float
                         int nmat, const int* mat_i, const float* mat_f, int ntex, const int* tex_wh,
                         const float* tex_data, int env_tex, float env_gain, int build_threads);
 void port_scene_destroy(void* scene);
+int port_scene_set_materials(void* scene, int nmat, const int* mat_i, const float* mat_f);
 
 // Depth-first export of the BVH (same layout as the reference harness).
 int port_bvh_export(void* scene, float* box, int* kids, int* leaf_first, int* leaf_count, int* leaf_tris,

@@ -6,7 +6,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 
-REF_ROOT = "/root/reference"
+from oracle.bind import REF_ROOT  # noqa: E402  (the reference checkout, NURAY_REF_ROOT)
 
 
 def pytest_configure(config):
@@ -25,7 +25,7 @@ def ref_lib():
     from oracle import bind
     if os.path.exists(bind.REF_LIB):
         return bind.REF_LIB
-    path = bind.build_ref(REF_ROOT)
+    path = bind.build_ref()
     if path is None:
         pytest.skip("reference sources not present on this machine")
     return path

@@ -15,6 +15,12 @@ Fixtures (all small .npz files):
   small_*.npz            the same for the seeded mixed-material scene of
                          nuray_gb300.scenes.small_scene(), plus material,
                          light-pick and texture probes
+  cornell_render_rgb8.npz  the 8-bit image of RendererPTLS::render itself
+                         (oracle/ref_render.cpp: the reference's frame loop
+                         on the Philox stream) for the Cornell workload,
+                         320x240 at 16 spp
+
+    python tests/golden/make_golden.py [/path/to/reference] [--only render]
 """
 import os
 import sys
@@ -78,9 +84,26 @@ def probe_inputs(n, seed):
     return wo, nrm, wi, uv, u
 
 
-def main(ref_root):
+def render_fixture():
+    """RendererPTLS::render's 8-bit output (src/renderer/rendererptls.cpp:165-181:
+    per-sample max(0, L), the mean, pow(1/2.2), x255, clamp, qRgb's
+    truncation) for the Cornell workload, seed 0."""
+    g = dict(np.load(os.path.join(OUT, "cornell_scene.npz")))
+    mats = [dict(type=int(i[0]), c0=f[0:3].tolist(), c1=f[3:6].tolist(), alpha=float(f[6]), ior=float(f[7]),
+                 ns=float(f[8])) for i, f in zip(g["mat_i"], g["mat_f"])]
+    sc = dict(pos=g["pos"], uv=g["uv"], nrm=g["nrm"], mat=g["mat"], mats=mats)
+    rgb8 = bind.ref_render_image(sc, CORNELL_PARAMS, seed=0)
+    np.savez_compressed(os.path.join(OUT, "cornell_render_rgb8.npz"), rgb8=rgb8, params=np.array(CORNELL_PARAMS),
+                        seed=np.uint64(0))
+
+
+def main(ref_root, only=None):
     if bind.build_ref(ref_root) is None:
         sys.exit("reference sources not found at " + ref_root)
+    if only == "render":
+        render_fixture()
+        print("fixture written to", OUT)
+        return
     desc = os.path.join(ref_root, "scenes/cornell/CornellBox-Original.obj") + " -s 100\n"
     R = bind.Oracle("ref", desc=desc)
     sc = ref_scene_arrays(R)
@@ -124,8 +147,13 @@ def main(ref_root):
                         params=np.array(s["params"]), wo=wo, nrm=nrm, wi=wi, uv=uv, u=u, light_u=ul,
                         light_tri=ltri, light_p=np.float32(lp), tex_mat=np.int32(tex_mat), tex_uv=tuv,
                         tex_rgb=tex, env_rgb=env, **probes)
+    render_fixture()
     print("fixtures written to", OUT)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only:
+        args = [a for a in args if a != only]
+    main(args[0] if args else bind.REF_ROOT, only)

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import shim
-from conftest import ROOT, golden
+from conftest import REF_ROOT, ROOT, golden
 from nuray_gb300 import scenes
 
 
@@ -96,7 +96,7 @@ def test_bvh_builder_parallel_is_deterministic(host, port_lib):
 
 
 def test_loader_matches_reference_loader_fixture(host):
-    ref = "/root/reference/scenes/cornell/CornellBox-Original.obj"
+    ref = os.path.join(REF_ROOT, "scenes/cornell/CornellBox-Original.obj")
     if not os.path.exists(ref):
         pytest.skip("reference scenes not present")
     pos, uv, nrm, mat, mats = shim.load_scene(host, ref + " -s 100\n")

@@ -6,13 +6,14 @@ committed fixtures (generated from the reference by tests/golden/make_golden.py)
 it must agree bit for bit on x86 and within a few ulps elsewhere (libm
 differences between architectures).
 """
+import os
 import platform
 
 import numpy as np
 import pytest
 
 from conftest import golden
-from oracle.bind import Oracle, pixel_grid
+from oracle.bind import REF_ROOT, Oracle, pixel_grid
 from nuray_gb300 import scenes
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
@@ -98,7 +99,7 @@ def test_port_probes_match_golden(port_lib):
 
 def test_port_equals_reference_cornell_full(port_lib, ref_lib):
     import os
-    R = Oracle("ref", desc=os.path.join("/root/reference/scenes/cornell/CornellBox-Original.obj") + " -s 100\n")
+    R = Oracle("ref", desc=os.path.join(REF_ROOT, "scenes/cornell/CornellBox-Original.obj") + " -s 100\n")
     P = Oracle("port", cornell_scene())
     params = "renderer=ptnee imgw=80 imgh=60 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
     pix = pixel_grid(80, 60)
@@ -196,9 +197,53 @@ def test_port_equals_reference_nrc_estimator(port_lib, ref_lib, seed):
 
 def test_port_equals_reference_nrc_estimator_cornell(port_lib, ref_lib):
     import os
-    R = Oracle("ref", desc=os.path.join("/root/reference/scenes/cornell/CornellBox-Original.obj") + " -s 100\n")
+    R = Oracle("ref", desc=os.path.join(REF_ROOT, "scenes/cornell/CornellBox-Original.obj") + " -s 100\n")
     P = Oracle("port", cornell_scene())
     params = ("renderer=nrc imgw=80 imgh=60 spp=16 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333 "
               "path_lim=1000000")
     pix = pixel_grid(80, 60)
     np.testing.assert_array_equal(P.render_samples(params, pix, 4, seed=11), R.render_samples(params, pix, 4, seed=11))
+
+
+def rgb8_from_samples(samples):
+    """RendererPTLS::render's per-pixel arithmetic (src/renderer/rendererptls.cpp:170-180)
+    on per-sample radiance already clamped at 0: float sums in sample order, the
+    mean, powf(., 1/2.2), x255, clamp to [0, 255] and qRgb's truncation."""
+    s = np.zeros(samples.shape[::2], np.float32)
+    for i in range(samples.shape[1]):
+        s = (s + samples[:, i]).astype(np.float32)
+    m = (s / np.float32(samples.shape[1])).astype(np.float32)
+    p = (np.power(m, np.float32(1.0 / 2.2)).astype(np.float32) * np.float32(255)).astype(np.float32)
+    return np.clip(p, 0, 255).astype(np.int32)
+
+
+def test_render_rgb8_fixture_from_port(port_lib):
+    """The 8-bit image of the reference's own render() (fixture) equals the
+    restatement's per-sample radiance put through render()'s per-pixel
+    arithmetic: exactly on x86, within one level elsewhere."""
+    g = golden("cornell_render_rgb8.npz")
+    params = str(g["params"])
+    P = Oracle("port", cornell_scene())
+    w, h = 320, 240
+    want = g["rgb8"].astype(np.int32).reshape(-1, 3)
+    got = rgb8_from_samples(P.render_samples(params, pixel_grid(w, h), 16, seed=int(g["seed"])))
+    if EXACT:
+        np.testing.assert_array_equal(got, want)
+    else:
+        assert np.abs(got - want).max() <= 1 and np.mean(got == want) > 0.99
+
+
+def test_reference_render_loop_equals_its_samples(ref_lib):
+    """The harness that runs render() whole (oracle/ref_render.cpp) draws each
+    sample's uniforms exactly as the per-sample harness: its image equals the
+    per-sample radiance of the reference's trace() put through render()'s
+    per-pixel arithmetic, bit for bit."""
+    from oracle.bind import REF_RENDER_LIB, ref_render_image
+    if not os.path.exists(REF_RENDER_LIB):
+        pytest.skip("reference render harness not built")
+    sc = cornell_scene()
+    params = "renderer=ptnee imgw=48 imgh=40 spp=6 campos=0,120,200 cameuler=0,0,0 camfov=64 camasp=1.333"
+    img = ref_render_image(sc, params, seed=5).astype(np.int32).reshape(-1, 3)
+    R = Oracle("ref", sc)
+    want = rgb8_from_samples(R.render_samples(params, pixel_grid(48, 40), 6, seed=5))
+    np.testing.assert_array_equal(img, want)

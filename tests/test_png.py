@@ -17,6 +17,7 @@ import numpy as np
 import pytest
 
 import shim
+from conftest import REF_ROOT
 
 ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
 CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
@@ -245,7 +246,7 @@ def python_png_decode(data):
 
 @pytest.mark.parametrize("name", ["default.png", "mitsuba-icon.png"])
 def test_reference_scene_textures(L, name):
-    path = os.path.join("/root/reference/scenes/mitsuba", name)
+    path = os.path.join(REF_ROOT, "scenes/mitsuba", name)
     if not os.path.exists(path):
         pytest.skip("reference checkout not present")
     data = open(path, "rb").read()
@@ -262,7 +263,7 @@ def test_loader_reads_reference_scene_with_png_texture(L, ref_lib):
     Texture::load's values of the decoded image."""
     import ctypes
     from oracle.bind import Oracle
-    obj = "/root/reference/scenes/mitsuba/mitsuba-back.obj"
+    obj = os.path.join(REF_ROOT, "scenes/mitsuba/mitsuba-back.obj")
     pos, uv, nrm, mat, mats = shim.load_scene(L, obj + "\n")
     R = Oracle("ref", desc=obj + "\n")
     n = R.L.ref_scene_num_tris(ctypes.c_void_p(R.h))
@@ -275,8 +276,8 @@ def test_loader_reads_reference_scene_with_png_texture(L, ref_lib):
     np.testing.assert_array_equal(nrm, rn)
     textured = [m for m in mats if m.tex0 >= 0]
     assert len(textured) == 1 and textured[0].type == 4  # BlinnPhong (Ks 0.2) with map_Kd
-    tex = shim.read_image(L, "/root/reference/scenes/mitsuba/default.png")
-    rgb = python_png_decode(open("/root/reference/scenes/mitsuba/default.png", "rb").read())
+    tex = shim.read_image(L, os.path.join(REF_ROOT, "scenes/mitsuba/default.png"))
+    rgb = python_png_decode(open(os.path.join(REF_ROOT, "scenes/mitsuba/default.png"), "rb").read())
     want = np.power((rgb.astype(np.int64) * 257).astype(np.float64) / 65535.0,
                     np.float64(np.float32(2.2))).astype(np.float32)
     np.testing.assert_array_equal(tex, want)
