@@ -14,8 +14,15 @@ value: paths / s with the scene resident and the image left on the device
 (nr_render with no host output), timed with CUDA events on the library's
 stream. e2e: the same render through nr_render with a pinned host output
 image, so the 24.9 MB device-to-host copy is inside the timed region.
-time_to_relmse (after the timed steps, not part of `value`): the metric's
-second half, plain PT against PT + the online neural radiance cache.
+roofline: k_trace's algorithmic bytes (32 B per visited node, 36 B per
+tested triangle) per second against the measured copy bandwidth; beside it
+the issue roofline of k_trace and k_shadow (both issue-bound), and the whole
+path's bytes. c3 / c5_adjoint (after the timed steps, own clocks): frames of
+the third workload (sky with importance sampling, textures, dielectrics, 256
+spp) and gradients of the inverse-rendering workload, timed the same way.
+time_to_relmse (not part of `value`): the metric's second half, plain PT
+against PT + the online neural radiance cache, at 1920x1080 and 64 spp per
+frame (the fourth workload), and at 960x540 and 1 spp per frame.
 
 Multi-GPU (torchrun): every rank renders its own 64-sample range of the
 frame (sample0 = 64 * rank) with no collective on the data path (weak
@@ -42,17 +49,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 MEASURED = os.path.join(ROOT, "MEASURED_PEAKS.json")
-BYTES_NODE = 64      # one internal node: both child boxes + references
-BYTES_TRI = 48       # one triangle: p0, e1, e2 (+ ids)
-BYTES_RAY_IO = 72    # queue entry, ray origin/direction, hit record, sort entry, material type
-# DRAM bytes (read + write) per closest-hit ray of k_trace, from one ncu
-# capture of a bounce-0 launch (profiles/k_trace_c2_first_bounce.md); the
-# roofline's `traffic` scales it to a full launch by rays per launch.
-TRACE_DRAM_BYTES_PER_RAY = 62.2
-# cache hit rates of the same capture (lts__t_sector_hit_rate,
-# l1tex__t_sector_hit_rate), reported beside the roofline
-TRACE_L2_HIT_RATE = 0.675
-TRACE_L1_HIT_RATE = 0.796
+# Algorithmic bytes of the closest-hit walk: 32 B per visited node (one
+# FP32 child box) and 36 B per tested triangle (three FP32 vertices), times
+# the visits and tests counted by an instrumented frame of the workload.
+BYTES_NODE = 32
+BYTES_TRI = 36
+# Figures that come from one ncu capture of the workload, not from this run:
+# per bounce-0 closest-hit ray of k_trace, its DRAM bytes (read + write) and
+# cache sector hit rates; per ray of k_trace and k_shadow, their warp
+# instructions (smsp__inst_executed.sum over the launch's rays), which give
+# the issue roofline: instructions / (SMs x 4 schedulers x clock x time).
+NCU_CAPTURE = {
+    "what": "one ncu capture, 480x270 x 32 spp frame of the same scene, bounce-0 launches",
+    "k_trace": {"dram_bytes_per_ray": 62.2, "l2_hit_rate": 0.675, "l1_hit_rate": 0.796,
+                "warp_inst_per_ray": 185.7},
+    "k_shadow": {"warp_inst_per_ray": None},
+}
+SM_COUNT = 152
 
 
 def parse():
@@ -68,7 +81,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-tile-stride", type=int, default=4, help="CPU sample: every k-th 4x4 tile")
     ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE comparison")
-    ap.add_argument("--relmse-res", default="960x540")
+    ap.add_argument("--relmse-res", default="1920x1080",
+                    help="frame of the time-to-relMSE comparison at 64 spp per frame (the 1-spp-per-frame leg "
+                         "runs at 960x540)")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the third workload's frame and the adjoint leg of the default line")
     ap.add_argument("--nrc", default=None, metavar="PARAMS",
                     help="each step is a PT + NRC frame: a fresh cache is attached and the render gets "
                          "'nrc=1 nrc_train=16384 PARAMS' (measures the cache's per-frame cost)")
@@ -198,24 +215,29 @@ def cpu_leg(sc, params, spp, w, h, stride, budget_s=20.0):
     return n * spp / dt / 1e6, desc, threads
 
 
-def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0, spf=64):
+def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0, spf=64, res_1spp="960x540"):
     """Second half of the metric: wall time (CUDA events) to relMSE <= 1e-3
     against a converged render, plain PT against PT + the online neural
     radiance cache, both progressive with the same frame size: `spf`
     samples per pixel per frame (64: near the fastest frame size of either
-    method on this scene), and one sample per pixel per frame (the
-    real-time regime, where fixed per-frame costs weigh most)."""
+    method on this scene) on the `res` frame (the fourth workload's
+    1920x1080), and one sample per pixel per frame on a `res_1spp` frame
+    (the real-time regime, where fixed per-frame costs weigh most)."""
     from nuray_gb300 import convergence as C
-    w, h = res.split("x")
-    p = params.replace("imgw=1920", f"imgw={w}").replace("imgh=1080", f"imgh={h}")
-    ref = C.reference(S, p, ref_spp)
     out = {"target": target, "resolution": res, "reference_spp": ref_spp, "unit": "ms", "spp_per_frame": spf}
-    for k, label in ((spf, None), (1, "at_1_spp_per_frame")):
+    refs = {}
+    for k, r, label in ((spf, res, None), (1, res_1spp, "at_1_spp_per_frame")):
+        w, h = r.split("x")
+        p = params.replace("imgw=1920", f"imgw={w}").replace("imgh=1080", f"imgh={h}")
+        if r not in refs:
+            refs[r] = C.reference(S, p, ref_spp)
+        ref = refs[r]
         pt_curve, pt_t = C.progressive(S, p, 100000, ref, target, time_limit_s=limit_s, spf=k)
         nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "nrc_train=16384", limit_s, warmup=max(1, 256 // k),
                                      spf=k)
         res_k = {"pt": C.summary(pt_curve, pt_t), "pt_nrc": C.summary(nrc_curve, nrc_t)}
         if label:
+            res_k["resolution"] = r
             out[label] = res_k
         else:
             out.update(res_k)
@@ -253,18 +275,19 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def run_adjoint(args, local):
-    """--workload c5: each step is one nr_adjoint call (a render pass that
-    records every bounce's hits and light-sample visibility, then the adjoint
-    replay of every path from those records) for a fixed seeded d loss / d
-    image; the per-material gradient comes back to the host inside the timed
-    region."""
+def adjoint_leg(steps, warmup, extra_params="", clock_index=0):
+    """One nr_adjoint call per step on the 200k-triangle, 64-material
+    inverse-rendering workload (512x512, 32 spp, depth 4, RR from 3): a
+    render pass that records every bounce's hits and light-sample visibility,
+    then the adjoint replay of every path from those records, for a fixed
+    seeded d loss / d image; the per-material gradient comes back to the
+    host inside the timed region. Returns the measurements and the clocks."""
     import torch
     from nuray_gb300 import Scene, build, inverse
     build.build()
     sc = inverse.c5_scene(0)
     S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"])
-    params = sc["params"] + (" " + args.params if args.params else "")
+    params = sc["params"] + (" " + extra_params if extra_params else "")
     w = h = 512
     spp = 32
     rng = np.random.default_rng(7)
@@ -272,21 +295,18 @@ def run_adjoint(args, local):
     S.render_device(params.replace("spp=32", "spp=1") + " count=1")
     cnt = S.stats()
     stream = torch.cuda.ExternalStream(S.stream())
-    for k in range(args.warmup):
+    for k in range(warmup):
         S.adjoint(params + f" seed={k + 1}", dl)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    with ClockSampler(clock_index) as clk:
         e0.record(stream)
-        for k in range(args.steps):
+        for k in range(steps):
             S.adjoint(params + f" seed={100 + k}", dl)
         e1.record(stream)
         e1.synchronize()
     ms = e0.elapsed_time(e1)
-    paths = w * h * spp * args.steps
-    value = paths / (ms / 1e3) / 1e6
-    pk, pk_kind = peaks()
-    peak = pk.get("hbm_gbs", 6800.0)
+    paths = w * h * spp * steps
     paths1 = max(1, cnt["paths"])
     b_path = ((32 * cnt["nodes_visited"] + 36 * cnt["tris_tested"] + 32 * cnt["shadow_nodes_visited"]
                + 36 * cnt["shadow_tris_tested"]) / paths1 + 240 * cnt["rays"] / paths1 + 12)
@@ -295,23 +315,68 @@ def run_adjoint(args, local):
     # read again, the shading reads (240 B) and the adjoint slot state (64 B)
     rays_pp = cnt["rays"] / paths1
     b_adj = b_path + rays_pp * (17 + 17 + 240 + 64) + 12
-    achieved = b_adj * paths / (ms / 1e3) / 1e9
-    out = {"metric": "Mpaths/s adjoint", "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": 1,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 2),
+    out = {"value": paths / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "paths_per_step": w * h * spp,
+           "bytes_per_path": b_adj, "gbs": b_adj * paths / (ms / 1e3) / 1e9,
+           "launches": steps * S.stats()["kernel_launches"],
+           "workload": f"path-replay adjoint, {sc['pos'].shape[0]} triangles, {len(sc['mats'])} materials, "
+                       f"{w}x{h}, spp={spp}, maxdepth 4, RR from depth 3"}
+    S.close()
+    return out, clk.summary()
+
+
+def run_adjoint(args, local):
+    """--workload c5: the adjoint leg as the line's own metric."""
+    r, clocks = adjoint_leg(args.steps, args.warmup, args.params, local)
+    pk, pk_kind = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    out = {"metric": "Mpaths/s adjoint", "value": round(r["value"], 3), "unit": "Mpaths/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 2),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded procedural scene, seeded d loss / d image)",
-           "config": {"workload": f"path-replay adjoint, {sc['pos'].shape[0]} triangles, {len(sc['mats'])} "
-                                  f"materials, {w}x{h}, spp={spp}, maxdepth 4, RR from depth 3",
-                      "paths_per_step": w * h * spp},
+           "config": {"workload": r["workload"], "paths_per_step": r["paths_per_step"]},
            "roofline": {"kernel": "render pass with hit records + recorded replay", "bound": "hbm",
-                        "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                        "frac": round(achieved / peak, 3), "peak_source": pk_kind, "traffic": None,
-                        "bytes_per_path": round(b_adj, 1),
+                        "achieved": round(r["gbs"], 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(r["gbs"] / peak, 3), "peak_source": pk_kind, "traffic": None,
+                        "bytes_per_path": round(r["bytes_per_path"], 1),
                         "formula": "ptnee path bytes + rays x (17 record write + 17 read + 240 shading + 64 adjoint "
                                    "state) + 12"},
-           "gpu_launches": args.steps * S.stats()["kernel_launches"], "cpu_baseline": None, "e2e": None,
-           "clocks": clk.summary()}
+           "gpu_launches": r["launches"], "cpu_baseline": None, "e2e": None, "clocks": clocks}
     print(json.dumps(out), flush=True)
+
+
+def c3_leg(steps, warmup, clock_index=0):
+    """Frames of the third workload (the 1M-triangle scene with the HDR sky
+    and its importance sampling, value-noise textures on half the materials,
+    10 % GGX dielectrics; 1920x1080 at 256 spp: four waves of 2^27 paths),
+    timed like the main frames."""
+    import torch
+    from nuray_gb300 import Scene, scenes
+    sc = scenes.with_env_textures(scenes.terrain_spheres(0), 0)
+    S = Scene.from_arrays(sc["pos"], sc["mat"], sc["mats"], uv=sc["uv"], nrm=sc["nrm"], textures=sc["textures"],
+                          env_tex=sc["env_tex"], env_gain=sc["env_gain"])
+    params = sc["params"] + " envis=1"
+    stream = torch.cuda.ExternalStream(S.stream())
+    for _ in range(warmup):
+        S.render_device(params)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    with ClockSampler(clock_index) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            S.render_device(params)
+            launches += S.stats()["kernel_launches"]
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    paths = 1920 * 1080 * 256
+    S.close()
+    return {"value": round(paths * steps / (ms / 1e3) / 1e6, 3), "unit": "Mpaths/s", "steps": steps,
+            "warmup": warmup, "ms_per_step": round(ms / steps, 2), "paths_per_step": paths, "gpu_launches": launches,
+            "workload": "procedural terrain+spheres, 991296 triangles, 1920x1080, spp=256, maxdepth 8, RR from depth "
+                        "3, 2048x1024 HDR sky (peak 5e3) with environment importance sampling (envis=1), 512x512 "
+                        "value-noise textures on half the materials, 10% GGX dielectrics",
+            "clocks": clk.summary()}
 
 
 def main():
@@ -369,13 +434,14 @@ def main():
 
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    trace_ms, trace_launches, rays, shadow_rays, launches = 0.0, 0, 0, 0, 0
+    trace_ms, shadow_ms, trace_launches, rays, shadow_rays, launches = 0.0, 0.0, 0, 0, 0, 0
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for k in range(args.steps):
             S.render_device(base + " profile=1")
             st = S.stats()
             trace_ms += st["kernel_ms_trace"]
+            shadow_ms += st["kernel_ms_shadow"]
             trace_launches += st["trace_launches"]
             rays += st["rays"]
             shadow_rays += st["shadow_rays"]
@@ -414,8 +480,11 @@ def main():
         return
 
     pk, pk_kind = peaks()
-    bytes_per_ray = (BYTES_NODE * cnt["nodes_visited"] + BYTES_TRI * cnt["tris_tested"]) / max(1, cnt["rays"]) \
-        + BYTES_RAY_IO
+    clocks = clk.summary()
+    # k_trace: the closest-hit walk's algorithmic bytes (32 B per visited
+    # node, 36 B per tested triangle, counts of an instrumented frame) per
+    # extension ray, x rays, / the summed CUDA-event time of its launches
+    bytes_per_ray = (BYTES_NODE * cnt["nodes_visited"] + BYTES_TRI * cnt["tris_tested"]) / max(1, cnt["rays"])
     trace_bytes = bytes_per_ray * rays
     achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
     peak = pk.get("hbm_gbs", 6800.0)
@@ -424,16 +493,30 @@ def main():
             "frac": round(achieved / peak, 3) if achieved else None, "peak_source": pk_kind,
             "traffic": None,
             "bytes_per_ray": round(bytes_per_ray, 1),
+            "bytes_formula": "32 B x nodes visited + 36 B x triangles tested per extension ray",
             "nodes_per_ray": round(cnt["nodes_visited"] / max(1, cnt["rays"]), 2),
             "tris_per_ray": round(cnt["tris_tested"] / max(1, cnt["rays"]), 2),
             "avg_launch_ms": round(trace_ms / max(1, trace_launches), 4),
             "share_of_step": round(trace_ms / ms, 3)}
-    roof["traffic"] = round(TRACE_DRAM_BYTES_PER_RAY * rays / max(1, trace_launches))
-    roof["traffic_note"] = ("ncu DRAM bytes per ray of a bounce-0 k_trace launch (small case of the same scene) "
-                            "x rays per launch")
-    roof["l2_hit_rate"] = TRACE_L2_HIT_RATE
-    roof["l1_hit_rate"] = TRACE_L1_HIT_RATE
-    roof["hit_rate_note"] = "ncu sector hit rates of the same bounce-0 k_trace capture"
+    tr = NCU_CAPTURE["k_trace"]
+    roof["traffic"] = round(tr["dram_bytes_per_ray"] * rays / max(1, trace_launches))
+    roof["ncu_capture"] = {"source": NCU_CAPTURE["what"] + " (constants, not measured in this run)",
+                           "dram_bytes_per_ray": tr["dram_bytes_per_ray"], "l2_hit_rate": tr["l2_hit_rate"],
+                           "l1_hit_rate": tr["l1_hit_rate"],
+                           "traffic_formula": "dram_bytes_per_ray x extension rays per launch"}
+    # issue roofline of the traversal kernels: warp instructions (per ray, from
+    # the capture) x rays / (SMs x 4 issue slots per clock x the sampled SM
+    # clock x the kernels' CUDA-event time)
+    mhz = clocks.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    issue = {"unit": "warp instructions / issue slot", "sm_mhz": mhz,
+             "formula": "warp_inst_per_ray x rays / (152 SMs x 4 x SM clock x kernel time)"}
+    for name, nrays, kms in (("k_trace", rays, trace_ms), ("k_shadow", shadow_rays, shadow_ms)):
+        ipr = NCU_CAPTURE[name]["warp_inst_per_ray"]
+        if ipr and kms > 0:
+            slots = SM_COUNT * 4 * mhz * 1e6 * kms / 1e3
+            issue[name] = {"warp_inst_per_ray": ipr, "frac": round(ipr * nrays / slots, 3),
+                           "kernel_ms_per_step": round(kms / args.steps, 2)}
+    roof["issue"] = issue
     # the whole path's algorithmic bytes, per path:
     # sum over rays (32 B per node, 36 B per triangle) + 240 B per shaded
     # vertex (hit attributes, material, path state, hit record) + 12 B film
@@ -463,9 +546,18 @@ def main():
                                        "gpu_device": round(bvh_gpu_dev_ms, 1)}},
            "rays_per_s": round((rays + shadow_rays) / (ms / 1e3), 1), "extension_rays": rays,
            "shadow_rays": shadow_rays, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
-           "e2e": e2e, "clocks": clk.summary()}
+           "e2e": e2e, "clocks": clocks}
     if e2e:
         out["gpu_launches_e2e"] = launches_e2e * args.steps
+    if not args.no_extra and world == 1 and args.workload == "c2" and cache is None:
+        # the other two GPU workloads, timed the same way (their own clocks)
+        out["c3"] = c3_leg(max(2, args.steps // 4), 1, local)
+        r, c5_clocks = adjoint_leg(max(5, args.steps), 2, "", local)
+        out["c5_adjoint"] = {"value": round(r["value"], 3), "unit": "Mpaths/s of gradient",
+                             "ms_per_step": round(r["ms_per_step"], 2), "paths_per_step": r["paths_per_step"],
+                             "steps": max(5, args.steps), "warmup": 2, "gpu_launches": r["launches"],
+                             "workload": r["workload"], "hbm_gbs": round(r["gbs"], 1),
+                             "bytes_per_path": round(r["bytes_per_path"], 1), "clocks": c5_clocks}
     if not args.no_relmse and world == 1:
         out["time_to_relmse"] = relmse_leg(S, params, args.relmse_res)
     print(json.dumps(out), flush=True)

@@ -173,7 +173,13 @@ int nr_scene_info(const nr_scene* scene, int64_t info[6]);
  * builds it on the device, level by level: the same cost and split rule,
  * the same tree wherever no two triangles share a pMax coordinate, and a
  * stable (loader-index) order among equal keys where the reference's
- * std::sort order is unspecified. No reference counterpart for the option. */
+ * std::sort order is unspecified. max_device_bytes=N caps the device memory
+ * the scene's own buffers may hold (scene data, path state, films, staging;
+ * not an attached cache): an allocation past it fails with NR_ERR_OOM, as a
+ * failed cudaMalloc does, and the scene stays usable for calls that fit.
+ * No reference counterpart for either option. Scenes whose positions,
+ * normals, texture coordinates, material parameters, texels or environment
+ * gain are not finite are refused with NR_ERR_INVALID. */
 int nr_scene_create_opts(const nr_scene_desc* desc, const char* options, nr_scene** out);
 int nr_scene_load_opts(const char* text, const char* options, nr_scene** out);
 
@@ -194,11 +200,18 @@ int nr_scene_export(const nr_scene* scene, float* pos, float* uv, float* nrm, in
 int nr_bvh_export(const nr_scene* scene, float* box, int32_t* kids, int32_t* leaf_first, int32_t* leaf_count,
                   int32_t* leaf_tris, int32_t* num_nodes, int32_t* num_leaf_tris);
 
-#define NR_PTR_DEVICE 1  /* flag: the ray and hit arrays are device pointers */
+#define NR_PTR_DEVICE 1          /* flag: the ray and hit arrays are device pointers */
+#define NR_INTERSECT_EXHAUSTIVE 2 /* flag: visit every node whose box the ray enters, as the reference's
+                                     BVH::_traversal does (src/hierarchy/bvh.cpp:99-127), instead of
+                                     skipping subtrees entered beyond 1.001 x the best hit so far */
 
 /* Closest hit for n rays (o, d: 3 floats each). tri receives the triangle
  * index in loader order or -1 for a miss (t = 1e18, b1 = b2 = 0), as
- * BVH::intersection does. */
+ * BVH::intersection does. The default walk skips subtrees that cannot hold
+ * a nearer hit; it returns the reference's hit except where the ray crosses
+ * a triangle at a grazing angle (|s1.e1| below about 1e-3, where the
+ * reference's determinant bias 1e-6 lets the triangle report a t short of
+ * its own box), which NR_INTERSECT_EXHAUSTIVE covers too. */
 int nr_intersect(nr_scene* scene, int32_t n, const float* o, const float* d, int32_t* tri, float* t, float* b1,
                  float* b2, int32_t flags);
 
@@ -212,14 +225,18 @@ int nr_camera_from_params(const char* params, nr_camera* cam);
  * run: hosts that hand a plugin a fixed memory budget at start-up, or
  * real-time loops that cannot take cudaMalloc's implicit device
  * synchronisation mid-frame. Rays and results go through one static device
- * array of NR_NOALLOC_MAX_RAYS (65,536) rays, 2.6 MB, reserved on every device
- * that loads the library until the process exits; larger n is rejected with
- * NR_ERR_INVALID (split the batch). The scene itself must already exist.
- * The first call on a device looks up the array's device address (with that
- * device current); make that first call before any stream capture. All calls
- * share the array, which keeps the last call's contents; calls whose work
- * overlapped on the GPU would race on it, so the library serialises them and
- * returns only once the results are on the host. */
+ * array of NR_NOALLOC_MAX_RAYS (65,536) rays, 2.6 MB. Under CUDA's lazy
+ * module loading that array is reserved on a device when the first scene is
+ * created there (nr_scene_create / nr_scene_load load its module and look up
+ * its device address, with that device current), and it stays reserved until
+ * the process exits; the calls themselves then load and allocate nothing.
+ * Larger n is rejected with NR_ERR_INVALID (split the batch). All calls share
+ * the array, which keeps the last call's contents; calls whose work overlapped
+ * on the GPU would race on it, so the library serialises them under one
+ * process-wide lock. Each call blocks until the results are on the host (it
+ * synchronises the scene's stream and copies into pageable memory), so it must
+ * not be called while the scene's stream, or any stream in a process-wide
+ * capture, is being captured into a CUDA graph. */
 #define NR_NOALLOC_MAX_RAYS 65536
 int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float* d, int32_t* tri, float* t, float* b1,
                          float* b2);
@@ -253,6 +270,10 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * for smaller ones), tail (waves of at most 2^22 paths: after this many
  * wavefront bounces one launch takes every live path to its end, tracing
  * its light samples inline; default 2, 0 never; the image is the same),
+ * prune (1, the default: a traversal skips subtrees entered beyond 1.001 x
+ * its best hit so far or its shadow ray's length; 0: every node whose box a
+ * ray enters is visited, as the reference's exhaustive BVH::_traversal, for
+ * the reference's hits on grazing rays as well; see nr_intersect),
  * envis=1 (ptnee only, no reference counterpart: one environment light
  * sample per light-sampling vertex besides the area-light sample, weighted
  * against BSDF-sampled misses by the balance heuristic; the same expected
@@ -296,14 +317,41 @@ typedef struct nr_nrc nr_nrc;
 /* params: lr (1e-3), beta1 (0.9), beta2 (0.99), eps (1e-8), seed (0, for the
  * Glorot-uniform initialisation), ema (0.99: renders query an exponential
  * moving average of the weights over Adam steps, 0 queries the current
- * weights). Allocates on the current device. nr_nrc_infer and the
- * gradient calls use the current weights. */
+ * weights), tc (1: the tcgen05 kernels for the forward and the data
+ * gradients, the default; 0: mma.sync throughout), tc_first_wait (polls of
+ * the first bounded wait for a group of tensor-core MMAs, default and maximum
+ * 4194304; 0 makes every such wait time out at once, to exercise the
+ * timeout path: the call then fails with NR_ERR_DEVICE, error bit 8, after
+ * the kernel has waited again for its MMAs and freed its tensor memory).
+ * Allocates on the current device. nr_nrc_infer and the gradient calls use
+ * the current weights. */
 int nr_nrc_create(const char* params, nr_nrc** out);
 int nr_nrc_destroy(nr_nrc* nrc);
 /* Number of FP32 parameters (weights and biases, layout in nrc.h). */
 int nr_nrc_num_params(int64_t* n);
 int nr_nrc_get_params(nr_nrc* nrc, float* params);
 int nr_nrc_set_params(nr_nrc* nrc, const float* params);
+/* The cache's whole training state, for checkpoint and resume (the
+ * reference's network has no optimizer state to save). which selects one
+ * array of nr_nrc_num_params floats: the FP32 parameters, the accumulated
+ * gradient (zero between training calls), Adam's first and second moments,
+ * the running sum of the moving average, the inference copy (that sum with
+ * its start-up correction, what renders query), or, read only, the BF16
+ * copies of the parameters and of the inference copy (widened to float); or
+ * NR_NRC_STATE_STEP, one float holding the Adam step count, which sets the
+ * bias corrections of the next step. Setting the parameters or the
+ * inference copy refreshes its BF16 copy. */
+#define NR_NRC_STATE_PARAMS 0
+#define NR_NRC_STATE_GRAD 1
+#define NR_NRC_STATE_M 2
+#define NR_NRC_STATE_V 3
+#define NR_NRC_STATE_EMA 4
+#define NR_NRC_STATE_INFER 5
+#define NR_NRC_STATE_PARAMS_BF16 6
+#define NR_NRC_STATE_INFER_BF16 7
+#define NR_NRC_STATE_STEP 8
+int nr_nrc_get_state(nr_nrc* nrc, int32_t which, float* out);
+int nr_nrc_set_state(nr_nrc* nrc, int32_t which, const float* in);
 /* Forward pass for n rows of NR_NRC_INPUTS floats (rounded to BF16); out n*3. */
 int nr_nrc_infer(nr_nrc* nrc, int32_t n, const float* x, float* out);
 /* Gradient of the loss over n rows (no update): grad receives
@@ -344,10 +392,13 @@ int nr_scene_set_materials(nr_scene* scene, int32_t n, const nr_material* mats);
  * that nr_render returns for the same params), writes d loss / d params
  * into dL_dparams: 7 floats per material (albedo r, g, b; roughness;
  * emission r, g, b). Each wave of paths is rendered once, recording every
- * bounce's hits and light-sample visibility, then replayed from its Philox
- * keys and those records (params adj=mega: one thread per path, re-traced
- * instead). image (may be NULL) receives the primal image of the same
- * samples. */
+ * bounce's hits and light-sample visibility (17 bytes per path and bounce,
+ * at most adj_records bytes, default 32 GiB), then replayed from its Philox
+ * keys and those records; bounces past the records are traced again.
+ * adj_records=0 keeps no records: every path is recomputed from its Philox
+ * keys alone (the same gradients, more tracing, no memory beyond a wave's
+ * path state). adj=mega replays each path in one thread, re-traced. image
+ * (may be NULL) receives the primal image of the same samples. */
 int nr_adjoint(nr_scene* scene, const nr_camera* cam, const char* params, const float* dL_dimage, float* dL_dparams,
                float* image);
 

@@ -15,6 +15,7 @@ NR_OK = 0
 ERRORS = {-1: "NR_ERR_INVALID", -2: "NR_ERR_CUDA", -3: "NR_ERR_OOM", -4: "NR_ERR_CANCELLED", -5: "NR_ERR_IO",
           -6: "NR_ERR_DEVICE"}
 NR_PTR_DEVICE = 1
+NR_INTERSECT_EXHAUSTIVE = 2
 
 MAT_LAMBERT, MAT_GGXR, MAT_GGX, MAT_GLASS, MAT_BLINNPHONG, MAT_LIGHT = range(6)
 
@@ -85,6 +86,8 @@ SIGNATURES = {
     "nr_scene_set_materials": [_vp, _i32, _vp],
     "nr_adjoint": [_vp, _vp, _cp, _vp, _vp, _vp],
     "nr_intersect_noalloc": [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
+    "nr_nrc_get_state": [_vp, _i32, _vp],
+    "nr_nrc_set_state": [_vp, _i32, _vp],
 }
 
 _lib = None
@@ -205,13 +208,16 @@ class Scene:
                                   ctypes.byref(nn), ctypes.byref(nt)))
         return box, kids, first, count, tris
 
-    def intersect(self, o, d):
+    def intersect(self, o, d, exhaustive=False):
+        """Closest hits (tri, t, b1, b2); exhaustive: visit every node whose
+        box the ray enters, as the reference does (NR_INTERSECT_EXHAUSTIVE)."""
         o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
         d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
         n = o.shape[0]
         tri = np.zeros(n, np.int32)
         t, b1, b2 = (np.zeros(n, np.float32) for _ in range(3))
-        check(lib().nr_intersect(self._h, n, _ptr(o), _ptr(d), _ptr(tri), _ptr(t), _ptr(b1), _ptr(b2), 0))
+        check(lib().nr_intersect(self._h, n, _ptr(o), _ptr(d), _ptr(tri), _ptr(t), _ptr(b1), _ptr(b2),
+                                 NR_INTERSECT_EXHAUSTIVE if exhaustive else 0))
         return tri, t, b1, b2
 
     def intersect_device(self, n, o_ptr, d_ptr, tri_ptr, t_ptr, b1_ptr, b2_ptr):

@@ -57,17 +57,35 @@ int guarded(F&& f) {
     }
 }
 
+// Device bytes a scene may hold (scene option max_device_bytes): every
+// buffer of the scene draws on it, and an allocation past it fails with
+// NR_ERR_OOM as a failed cudaMalloc does.
+struct Budget {
+    size_t cap = SIZE_MAX;
+    size_t used = 0;
+};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    Budget* budget = nullptr;
+    // Replaces the buffer by one of n bytes. Over the cap it throws before
+    // touching the old buffer; if cudaMalloc fails the buffer is left empty,
+    // so callers that cache sizes or pointers into it reset them first.
     void alloc(size_t n) {
+        if (budget && n > budget->cap - (budget->used - bytes))
+            throw NrError(NR_ERR_OOM, "device allocation of " + std::to_string(n) + " bytes exceeds the scene's cap of " +
+                                          std::to_string(budget->cap) + " bytes (" +
+                                          std::to_string(budget->used - bytes) + " in use)");
         release();
         if (n == 0) return;
         NR_CUDA(cudaMalloc(&p, n));
         bytes = n;
+        if (budget) budget->used += n;
     }
     void release() {
         if (p) cudaFree(p);
+        if (budget) budget->used -= bytes;
         p = nullptr;
         bytes = 0;
     }
@@ -98,6 +116,10 @@ struct nr_nrc {
     float* xf = nullptr;  // FP32 staging of caller inputs
     float* loss_host = nullptr;  // pinned
     bool tc = true;              // inference on tcgen05 (nrc_tc.cu); false: mma.sync (nrc.cu)
+    uint32_t tc_first_wait = NR_TC_FIRST_WAIT_LIMIT;  // bound of the first MMA wait of a layer
+    // the tensor-core kernels, unless disabled here or, after an unfinished
+    // MMA group (error bit 32), for the whole process
+    bool use_tc() const { return tc && nr::nrc_tc_enabled(); }
     DevBuf errbuf;               // error word of the tensor-core kernels
     DevBuf wt_img;               // packed transposed weights of the tensor-core backward pass
     uint32_t* err_host = nullptr;  // pinned
@@ -145,13 +167,21 @@ struct nr_scene {
     float* nrc_pred = nullptr;
     float nrc_last_loss = 0.f;
     double bvh_wall_ms = 0.0, bvh_device_ms = 0.0;  // last BVH build
+    Budget budget;
+
+    nr_scene() {
+        for (auto* b : all_bufs()) b->budget = &budget;
+    }
+    std::vector<DevBuf*> all_bufs() {
+        return {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_guide, &light_mat,
+                &adj_L, &adj_wave, &env_weight, &env_row_cdf, &env_col_cdf, &path_mem, &film, &out_hdr, &out_rgb8,
+                &pix_list, &scratch, &nrc_mem};
+    }
 
     ~nr_scene() {
         if (device >= 0) cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
-        for (auto* b : {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_guide, &light_mat, &path_mem,
-                        &film, &out_hdr, &out_rgb8, &pix_list, &scratch, &nrc_mem})
-            b->release();
+        for (auto* b : all_bufs()) b->release();
         if (counters_host) cudaFreeHost(counters_host);
         for (auto& e : ev_pool) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -321,6 +351,7 @@ void upload_scene(nr_scene* s) {
     D.env_gain = H.env_gain;
     D.max_depth = B.max_depth;
     D.num_nodes = ng;
+    D.prune_k = 1.0f + NR_PRUNE_MARGIN;
     if (n == 0) {
         D.root_ref = INT32_MIN;
     } else {
@@ -334,6 +365,14 @@ void finish_scene(nr_scene* s, const char* options) {
     const nr::Config opt(options ? options : "");
     const std::string bvh = opt.get_str("bvh");
     if (!bvh.empty() && bvh != "host" && bvh != "gpu") throw NrError(NR_ERR_INVALID, "bvh must be host or gpu");
+    const std::string cap = opt.get_str("max_device_bytes");
+    if (!cap.empty()) {
+        size_t used = 0;
+        unsigned long long v = 0;
+        try { v = std::stoull(cap, &used); } catch (const std::exception&) { used = 0; }
+        if (used != cap.size() || cap[0] == '-') throw NrError(NR_ERR_INVALID, "max_device_bytes must be a byte count");
+        s->budget.cap = (size_t)v;
+    }
     NR_CUDA(cudaGetDevice(&s->device));
     NR_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device));
     NR_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -352,6 +391,38 @@ void finish_scene(nr_scene* s, const char* options) {
         throw NrError(NR_ERR_INVALID, "BVH depth " + std::to_string(s->bvh.max_depth) + " exceeds the traversal stack");
     nr::launch_setup(s->num_sms);
     upload_scene(s);
+    // the static scratch of nr_intersect_noalloc: reserved and located on
+    // this device now, so that those calls load and allocate nothing (a
+    // failure here is reported by the first such call, which tries again)
+    (void)nr::noalloc_prepare(s->device);
+}
+
+// Drops every buffer a call grows for its own work (path state, films,
+// staging, the adjoint's records and the cache's record tables), keeping the
+// scene data: after an allocation failure the scene holds only what the next
+// call needs to start from.
+void release_work_buffers(nr_scene* s) {
+    cudaStreamSynchronize(s->stream);
+    for (auto* b : {&s->path_mem, &s->film, &s->out_hdr, &s->out_rgb8, &s->pix_list, &s->scratch, &s->adj_L,
+                    &s->adj_wave, &s->nrc_mem})
+        b->release();
+    s->capacity = 0;
+    s->sh_mult = 1;
+    s->film_pixels = 0;
+    s->film_samples = 0;
+    s->nrc_cap = s->nrc_tcap = 0;
+}
+
+// Runs f, a call's work on scene s; an allocation failure inside frees the
+// call's work buffers before it is reported.
+template <class F>
+void with_oom_release(nr_scene* s, F&& f) {
+    try {
+        f();
+    } catch (const NrError& e) {
+        if (e.code == NR_ERR_OOM) release_work_buffers(s);
+        throw;
+    }
 }
 
 // Sizes the path-state buffers for `cap` slots.
@@ -362,7 +433,14 @@ void ensure_paths(nr_scene* s, int cap, int sh_mult = 1) {
     const size_t C = (size_t)cap, CS = C * (size_t)sh_mult;
     const size_t f4 = 16;
     size_t bytes = C * f4 * 5 + C * 16 + C * 4 * 2 + C * 4 * nr::NUM_CAT + CS * f4 * 3 + nr::NUM_COUNTERS * 4 + 256 * 16;
-    s->path_mem.alloc(bytes);
+    const int old_cap = s->capacity;
+    s->capacity = 0;  // no slots while the buffer is replaced (an allocation may fail)
+    try {
+        s->path_mem.alloc(bytes);
+    } catch (...) {
+        if (s->path_mem.p) s->capacity = old_cap;  // refused by the cap: the old buffer is intact
+        throw;
+    }
     char* p = s->path_mem.as<char>();
     auto take = [&](size_t n) { char* r = p; p += (n + 255) & ~size_t(255); return r; };
     nr::PathState& P = s->ps;
@@ -412,10 +490,11 @@ void nrc_ensure_batch(nr_nrc* c, int m) {
 // word that receives bit 8 if a tensor-core wait timed out.
 void nrc_forward_backward(nr_nrc* c, const __nv_bfloat16* x, const float* y, const nr::NrcRows& R, uint32_t* err,
                           cudaStream_t st) {
-    if (c->tc) {
-        nr::nrc_launch_forward_tc(c->dev.wb, c->dev.params, x, R, c->out, c->num_sms, err, st, c->acts);
+    if (c->use_tc()) {
+        nr::nrc_launch_forward_tc(c->dev.wb, c->dev.params, x, R, c->out, c->num_sms, err, st, c->acts,
+                                  c->tc_first_wait);
         nr::nrc_launch_backward_data_tc(c->dev.wb, c->out, y, c->acts, c->dz, R, c->loss, c->num_sms, c->wt_img.p, err,
-                                        st);
+                                        st, c->tc_first_wait);
         nr::nrc_launch_backward_weight(c->dev, x, c->dz, c->acts, R, c->num_sms, st);
     } else {
         nr::nrc_launch_forward(c->dev, x, R, c->out, c->acts, c->num_sms, st);
@@ -432,7 +511,7 @@ void nrc_train_device(nr_nrc* c, const __nv_bfloat16* x, const float* y, int m, 
     nrc_forward_backward(c, x, y, R, c->errbuf.as<uint32_t>(), st);
     if (update) {
         c->step++;
-        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st);
+        nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st, c->errbuf.as<uint32_t>());
     }
 }
 
@@ -475,7 +554,18 @@ struct RenderArgs {
     int nrc_train_depth;  // > 0: training paths end in the cache from this depth on
     bool nrc_pre;         // renderer=nrc: one all-training pass before the samples (RendererNRC::render)
     bool adj_mega;        // adjoint replay as one thread per path (adj=mega) instead of the wavefront
+    bool prune;           // 0: every node whose box a ray enters is visited, as the reference does
+    int64_t adj_rec_bytes;  // the adjoint's per-bounce hit and visibility records: at most this many bytes
+                            // (0: none; the replay traces every bounce again from the Philox keys)
 };
+
+// The scene as the kernels of one call see it: the pruning factor of the
+// call's traversals.
+nr::DeviceScene scene_for(const nr_scene* s, bool prune) {
+    nr::DeviceScene D = s->dev;
+    D.prune_k = prune ? 1.0f + NR_PRUNE_MARGIN : INFINITY;
+    return D;
+}
 
 RenderArgs parse_args(const nr_camera* cam, const char* params) {
     nr::Config c(params);
@@ -493,6 +583,18 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.pol.imgh = c.get_int("imgh", 1);
     a.spp = c.get_int("spp", 1);
     a.pol.trav = c.get_int("trav", 1);
+    a.prune = c.get_int("prune", 1) != 0;
+    {
+        const std::string rec = c.get_str("adj_records");
+        a.adj_rec_bytes = int64_t(32) << 30;
+        if (!rec.empty()) {
+            size_t used = 0;
+            long long v = -1;
+            try { v = std::stoll(rec, &used); } catch (const std::exception&) { used = 0; }
+            if (used != rec.size() || v < 0) throw NrError(NR_ERR_INVALID, "adj_records must be a byte count >= 0");
+            a.adj_rec_bytes = v;
+        }
+    }
     // renderer=ptnee (RendererPTLS), pt (RendererPT, the same estimator without
     // light sampling) or nrc (RendererNRC: light samples without MIS, the
     // cache asked from vertex path_lim on, path_lim_train on training paths)
@@ -590,6 +692,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         if (cap > s->nrc_cap || tcap > s->nrc_tcap) {
             auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
             size_t C = (size_t)cap, T = (size_t)tcap;
+            s->nrc_cap = s->nrc_tcap = 0;  // set again once the records are in place
             s->nrc_mem.alloc(al(C * NRC_IN * 2) + al(C * 4) + al(C * 16) + al(T * NRC_IN * 2) + al(T * 4) + al(T * 16) * 2 +
                              256 + al(C * 12));
             char* p = s->nrc_mem.as<char>();
@@ -623,6 +726,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         nrc_ensure_batch(s->nrc, std::max(s->nrc_tcap, cap));
     }
     const float film_h = nr::film_height(A.cam);
+    const nr::DeviceScene D = scene_for(s, A.prune);
     auto t0 = std::chrono::steady_clock::now();
     int nrc_loss_pending = 0;  // training steps behind the loss copied to the cache's pinned buffer
     nr_stats& S = s->stats;
@@ -667,7 +771,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             if (A.pol.maxdepth > 0 && bounce >= A.pol.maxdepth) break;
             if (bounce >= kMaxBounces) throw NrError(NR_ERR_DEVICE, "paths still alive after 4096 bounces (prr = 1?)");
             if (tail && bounce >= A.tail) {
-                nr::launch_tail(P, s->dev, A.pol, cap, use_nrc ? &s->nrc_ctx : nullptr, st);
+                nr::launch_tail(P, D, A.pol, cap, use_nrc ? &s->nrc_ctx : nullptr, st);
                 S.kernel_launches += 1;
                 break;
             }
@@ -682,7 +786,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                 ev_kind.push_back(-1); ev_kind.push_back(0); ev_kind.push_back(1); ev_kind.push_back(2);
                 nev += 4;
             }
-            nr::launch_bounce(P, s->dev, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count,
+            nr::launch_bounce(P, D, A.pol, cap, live, st, A.profile ? evs : nullptr, A.count,
                               use_nrc ? &s->nrc_ctx : nullptr);
             std::swap(P.queue_in, P.queue_out);
             S.bounces++;
@@ -703,10 +807,10 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             // launch reads them there, so the host never waits here.
             nr_nrc* c = s->nrc;
             const nr::NrcCtx& X = s->nrc_ctx;
-            if (c->tc)
+            if (c->use_tc())
                 nr::nrc_launch_forward_tc(c->dev.wb_inf, c->dev.pinf, (const __nv_bfloat16*)X.q_x,
                                           nr::nrc_rows_counted(&X.counters[0], cap, 0, 1), s->nrc_pred, c->num_sms,
-                                          s->ps.counters + nr::CNT_ERR, st);
+                                          s->ps.counters + nr::CNT_ERR, st, nullptr, c->tc_first_wait);
             else
                 nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)X.q_x,
                                            nr::nrc_rows_counted(&X.counters[0], cap, 0, 1), s->nrc_pred, c->num_sms, st);
@@ -719,7 +823,8 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
                 const __nv_bfloat16* x = (const __nv_bfloat16*)X.t_x;
                 nrc_forward_backward(c, x, c->y, R, s->ps.counters + nr::CNT_ERR, st);
                 c->step++;
-                nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st);
+                nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, R, st,
+                                    s->ps.counters + nr::CNT_ERR);
             }
             NR_CUDA(cudaMemcpyAsync(c->loss_host, c->loss, 4, cudaMemcpyDeviceToHost, st));
             nrc_loss_pending = steps;
@@ -757,9 +862,16 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         *dst[ev_kind[i]] += ms;
     }
     S.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (c[nr::CNT_ERR] != 0)
-        throw NrError(NR_ERR_DEVICE, "device error bits " + std::to_string(c[nr::CNT_ERR]) +
-                                         " (1 stack overflow, 2 step cap, 4 shadow queue full, 8 tensor-core wait timed out)");
+    if (c[nr::CNT_ERR] != 0) {
+        if (c[nr::CNT_ERR] & nr::NR_ERRBIT_TC_LOST) nr::nrc_tc_disable();
+        // the cache skipped the update of a failed step: drop its gradient too
+        if (use_nrc) {
+            NR_CUDA(cudaMemsetAsync(s->nrc->dev.grad, 0, NRC_NUM_PARAMS * 4, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+        }
+        throw NrError(NR_ERR_DEVICE, "device error bits " + std::to_string(c[nr::CNT_ERR]) + " (" + nr::err_bits_text() +
+                                         ")");
+    }
 }
 
 // Both passes of the adjoint on the wavefront, wave by wave. Pass 1 renders
@@ -779,10 +891,11 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
     // slots, and shadow rays per bounce (one per path at most), of this wave size
     const size_t C = (size_t)std::max(cap, 1), CS = C;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    // recorded bounces: maxdepth, or 16 without one; at most 32 GiB of records
+    // recorded bounces: maxdepth, or 16 without one; at most adj_records bytes
+    // of records (32 GiB by default; 0: none, every bounce traced again)
     int depth_rec = A.pol.maxdepth > 0 ? A.pol.maxdepth : 16;
     const size_t per_bounce = al(C * 16) + al(C);
-    depth_rec = (int)std::max<size_t>(1, std::min<size_t>((size_t)depth_rec, (size_t(32) << 30) / per_bounce));
+    depth_rec = (int)std::min<size_t>((size_t)depth_rec, (size_t)A.adj_rec_bytes / per_bounce);
     s->adj_wave.ensure(al(C * 16) * 4 + al(CS * 16) * 2 + per_bounce * (size_t)depth_rec);
     char* p = s->adj_wave.as<char>();
     auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
@@ -796,6 +909,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
     float4* rec_hit = (float4*)take(C * 16 * (size_t)depth_rec);
     uint8_t* rec_vis = (uint8_t*)take(C * (size_t)depth_rec);
     const float film_h = nr::film_height(A.cam);
+    const nr::DeviceScene D = scene_for(s, A.prune);
     nr::Policy pol1 = A.pol;
     pol1.adj = 1;
     uint64_t launches = 0;
@@ -829,7 +943,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
             const bool rec = bounce < depth_rec;
             P.hit = rec ? rec_hit + (size_t)bounce * C : s->ps.hit;
             P.vis = rec ? rec_vis + (size_t)bounce * C : nullptr;
-            nr::launch_bounce(P, s->dev, pol1, cap, live, st, nullptr, false, nullptr);
+            nr::launch_bounce(P, D, pol1, cap, live, st, nullptr, false, nullptr);
             std::swap(P.queue_in, P.queue_out);
             launches += nr::bounce_launches(cap, false, s->dev.cat_mask);
             if (!live_after(bounce, live)) break;
@@ -850,12 +964,12 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
             if (rec) {
                 P.hit = rec_hit + (size_t)bounce * C;
                 vis = rec_vis + (size_t)bounce * C;
-                nr::launch_sort_recorded(P, s->dev, cap, st);
+                nr::launch_sort_recorded(P, D, cap, st);
             } else {
                 P.hit = s->ps.hit;
-                nr::launch_trace(P, s->dev, A.pol, cap, st);
+                nr::launch_trace(P, D, A.pol, cap, st);
             }
-            launches += 2 + nr::launch_adj_bounce_shading(P, s->dev, A.pol, cap, J, vis, d_grad, s->num_sms,
+            launches += 2 + nr::launch_adj_bounce_shading(P, D, A.pol, cap, J, vis, d_grad, s->num_sms,
                                                           nr::shadow_grid(), st);
             nr::launch_advance(P.counters, st);
             std::swap(P.queue_in, P.queue_out);
@@ -867,7 +981,7 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
     NR_CUDA(cudaGetLastError());
     if (s->counters_host[nr::CNT_ERR] != 0)
         throw NrError(NR_ERR_DEVICE, "device error bits " + std::to_string(s->counters_host[nr::CNT_ERR]) +
-                                         " in the adjoint (1 stack overflow, 2 step cap, 4 shadow queue full)");
+                                         " in the adjoint (" + nr::err_bits_text() + ")");
     return launches;
 }
 
@@ -925,6 +1039,9 @@ int nr_scene_destroy(nr_scene* s) {
 int nr_scene_set_env(nr_scene* s, int32_t width, int32_t height, const float* rgb, float gain) {
     return guarded([&]() {
         if (!s || width < 0 || height < 0 || (width > 0 && (height == 0 || !rgb))) throw NrError(NR_ERR_INVALID, "bad argument");
+        if (!std::isfinite(gain)) throw NrError(NR_ERR_INVALID, "env gain is not finite");
+        for (size_t i = 0; i < 3 * (size_t)width * height; ++i)
+            if (!std::isfinite(rgb[i])) throw NrError(NR_ERR_INVALID, "environment texel value " + std::to_string(i) + " is not finite");
         std::lock_guard<std::mutex> lk(s->mu);
         NR_CUDA(cudaSetDevice(s->device));
         nr::HostScene& H = s->host;
@@ -960,6 +1077,9 @@ int nr_scene_set_materials(nr_scene* s, int32_t n, const nr_material* mats) {
             if ((a.type == NR_MAT_LIGHT) != (b.type == NR_MAT_LIGHT)) throw NrError(NR_ERR_INVALID, "emitters cannot change");
             if (a.tex0 >= (int)s->host.tex_wh.size() / 2 || a.tex1 >= (int)s->host.tex_wh.size() / 2)
                 throw NrError(NR_ERR_INVALID, "material " + std::to_string(m) + ": texture index out of range");
+            const float f[9] = {a.c0[0], a.c0[1], a.c0[2], a.c1[0], a.c1[1], a.c1[2], a.alpha, a.ior, a.ns};
+            for (float x : f)
+                if (!std::isfinite(x)) throw NrError(NR_ERR_INVALID, "material " + std::to_string(m) + ": non-finite parameter");
         }
         std::lock_guard<std::mutex> lk(s->mu);
         NR_CUDA(cudaSetDevice(s->device));
@@ -973,62 +1093,64 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
     return guarded([&]() {
         if (!s || !dldi || !grad) throw NrError(NR_ERR_INVALID, "null argument");
         std::lock_guard<std::mutex> lk(s->mu);
-        NR_CUDA(cudaSetDevice(s->device));
-        RenderArgs A = parse_args(cam, params);
-        if (A.pol.excl) throw NrError(NR_ERR_INVALID, "the adjoint differentiates renderer=ptnee or pt");
-        if (A.pol.envis) throw NrError(NR_ERR_INVALID, "the adjoint does not support envis");
-        const int npix = A.pol.imgw * A.pol.imgh;
-        const int nm = (int)s->host.mats.size();
-        if ((size_t)nm * 7 * 4 > 200 * 1024) throw NrError(NR_ERR_INVALID, "too many materials for the adjoint (limit 7314)");
-        cudaStream_t st = s->stream;
-        size_t b_img = (size_t)npix * 12, b_grad = (size_t)nm * 7 * 4;
-        s->scratch.ensure(2 * b_img + b_grad + 3 * 256);
-        char* p = s->scratch.as<char>();
-        auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
-        float* d_dldi = (float*)take(b_img);
-        float* d_img = (float*)take(b_img);
-        float* d_grad = (float*)take(b_grad);
-        NR_CUDA(cudaMemcpyAsync(d_dldi, dldi, b_img, cudaMemcpyHostToDevice, st));
-        NR_CUDA(cudaMemsetAsync(d_img, 0, b_img, st));
-        NR_CUDA(cudaMemsetAsync(d_grad, 0, b_grad, st));
-        nr::AdjArgs J;
-        J.S = s->dev;
-        J.pol = A.pol;
-        J.cam = A.cam;
-        J.film_h = nr::film_height(A.cam);
-        J.npix = npix;
-        J.sample0 = (uint32_t)A.sample0;
-        J.spp = A.spp;
-        static bool attr = false;
-        if (!attr) {
-            nr::adjoint_setup();
-            attr = true;
-        }
-        auto t0 = std::chrono::steady_clock::now();
-        // every path's radiance (scanline pixel order, so the buffer index is
-        // (y * imgw + x) * spp + sample), then the replay of every path
-        s->adj_L.ensure((size_t)npix * A.spp * 12);
-        uint64_t launches = 0;
-        if (A.adj_mega) {
-            RenderArgs P1 = A;
-            P1.tile = 0;
-            P1.tail = 0;  // the wavefront to the end, as the wavefront adjoint's first pass
-            run_waves(s, P1, npix, nullptr, A.sample0, nullptr, s->adj_L.as<float>(), nullptr, nullptr, nullptr);
-            nr::launch_adjoint(J, d_dldi, d_grad, s->adj_L.as<float>(), s->num_sms, st);
-            launches = s->stats.kernel_launches + 1;
-        } else {
-            launches = adjoint_waves(s, A, npix, d_dldi, d_grad);
-        }
-        if (image) nr::launch_image_from_L(s->adj_L.as<float>(), npix, A.spp, d_img, st);
-        NR_CUDA(cudaGetLastError());
-        NR_CUDA(cudaMemcpyAsync(grad, d_grad, b_grad, cudaMemcpyDeviceToHost, st));
-        if (image) NR_CUDA(cudaMemcpyAsync(image, d_img, b_img, cudaMemcpyDeviceToHost, st));
-        NR_CUDA(cudaStreamSynchronize(st));
-        if (image) for (size_t i = 0; i < (size_t)npix * 3; ++i) image[i] /= (float)A.spp;
-        s->stats = nr_stats{};
-        s->stats.paths = (uint64_t)npix * A.spp;
-        s->stats.kernel_launches = launches + (image ? 1 : 0);
-        s->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        with_oom_release(s, [&]() {
+            NR_CUDA(cudaSetDevice(s->device));
+            RenderArgs A = parse_args(cam, params);
+            if (A.pol.excl) throw NrError(NR_ERR_INVALID, "the adjoint differentiates renderer=ptnee or pt");
+            if (A.pol.envis) throw NrError(NR_ERR_INVALID, "the adjoint does not support envis");
+            const int npix = A.pol.imgw * A.pol.imgh;
+            const int nm = (int)s->host.mats.size();
+            if ((size_t)nm * 7 * 4 > 200 * 1024) throw NrError(NR_ERR_INVALID, "too many materials for the adjoint (limit 7314)");
+            cudaStream_t st = s->stream;
+            size_t b_img = (size_t)npix * 12, b_grad = (size_t)nm * 7 * 4;
+            s->scratch.ensure(2 * b_img + b_grad + 3 * 256);
+            char* p = s->scratch.as<char>();
+            auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
+            float* d_dldi = (float*)take(b_img);
+            float* d_img = (float*)take(b_img);
+            float* d_grad = (float*)take(b_grad);
+            NR_CUDA(cudaMemcpyAsync(d_dldi, dldi, b_img, cudaMemcpyHostToDevice, st));
+            NR_CUDA(cudaMemsetAsync(d_img, 0, b_img, st));
+            NR_CUDA(cudaMemsetAsync(d_grad, 0, b_grad, st));
+            nr::AdjArgs J;
+            J.S = scene_for(s, A.prune);
+            J.pol = A.pol;
+            J.cam = A.cam;
+            J.film_h = nr::film_height(A.cam);
+            J.npix = npix;
+            J.sample0 = (uint32_t)A.sample0;
+            J.spp = A.spp;
+            static bool attr = false;
+            if (!attr) {
+                nr::adjoint_setup();
+                attr = true;
+            }
+            auto t0 = std::chrono::steady_clock::now();
+            // every path's radiance (scanline pixel order, so the buffer index is
+            // (y * imgw + x) * spp + sample), then the replay of every path
+            s->adj_L.ensure((size_t)npix * A.spp * 12);
+            uint64_t launches = 0;
+            if (A.adj_mega) {
+                RenderArgs P1 = A;
+                P1.tile = 0;
+                P1.tail = 0;  // the wavefront to the end, as the wavefront adjoint's first pass
+                run_waves(s, P1, npix, nullptr, A.sample0, nullptr, s->adj_L.as<float>(), nullptr, nullptr, nullptr);
+                nr::launch_adjoint(J, d_dldi, d_grad, s->adj_L.as<float>(), s->num_sms, st);
+                launches = s->stats.kernel_launches + 1;
+            } else {
+                launches = adjoint_waves(s, A, npix, d_dldi, d_grad);
+            }
+            if (image) nr::launch_image_from_L(s->adj_L.as<float>(), npix, A.spp, d_img, st);
+            NR_CUDA(cudaGetLastError());
+            NR_CUDA(cudaMemcpyAsync(grad, d_grad, b_grad, cudaMemcpyDeviceToHost, st));
+            if (image) NR_CUDA(cudaMemcpyAsync(image, d_img, b_img, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+            if (image) for (size_t i = 0; i < (size_t)npix * 3; ++i) image[i] /= (float)A.spp;
+            s->stats = nr_stats{};
+            s->stats.paths = (uint64_t)npix * A.spp;
+            s->stats.kernel_launches = launches + (image ? 1 : 0);
+            s->stats.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        });
     });
 }
 
@@ -1080,39 +1202,42 @@ int nr_intersect(nr_scene* s, int32_t n, const float* o, const float* d, int32_t
         if (!s || n < 0 || (n > 0 && (!o || !d || !tri || !t || !b1 || !b2))) throw NrError(NR_ERR_INVALID, "bad argument");
         if (n == 0) return;
         std::lock_guard<std::mutex> lk(s->mu);
-        NR_CUDA(cudaSetDevice(s->device));
-        ensure_paths(s, 1);
-        cudaStream_t st = s->stream;
-        const float *dO = o, *dD = d;
-        int32_t* dTri = tri;
-        float *dT = t, *dB1 = b1, *dB2 = b2;
-        if (!(flags & NR_PTR_DEVICE)) {
-            size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4;
-            s->scratch.ensure(2 * f3 + 4 * f1 + 6 * 256);  // six 256-byte aligned pieces
-            char* p = s->scratch.as<char>();
-            auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
-            float* xo = (float*)take(f3);
-            float* xd = (float*)take(f3);
-            dTri = (int32_t*)take(f1); dT = (float*)take(f1); dB1 = (float*)take(f1); dB2 = (float*)take(f1);
-            NR_CUDA(cudaMemcpyAsync(xo, o, f3, cudaMemcpyHostToDevice, st));
-            NR_CUDA(cudaMemcpyAsync(xd, d, f3, cudaMemcpyHostToDevice, st));
-            dO = xo; dD = xd;
-        }
-        NR_CUDA(cudaMemsetAsync(s->ps.counters + nr::CNT_ERR, 0, 4, st));
-        nr::launch_intersect(s->dev, n, dO, dD, dTri, dT, dB1, dB2, s->ps.counters + nr::CNT_ERR, st);
-        NR_CUDA(cudaGetLastError());
-        if (!(flags & NR_PTR_DEVICE)) {
-            size_t f1 = (size_t)n * 4;
-            NR_CUDA(cudaMemcpyAsync(tri, dTri, f1, cudaMemcpyDeviceToHost, st));
-            NR_CUDA(cudaMemcpyAsync(t, dT, f1, cudaMemcpyDeviceToHost, st));
-            NR_CUDA(cudaMemcpyAsync(b1, dB1, f1, cudaMemcpyDeviceToHost, st));
-            NR_CUDA(cudaMemcpyAsync(b2, dB2, f1, cudaMemcpyDeviceToHost, st));
-        }
-        uint32_t err = 0;
-        NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters + nr::CNT_ERR, 4, cudaMemcpyDeviceToHost, st));
-        NR_CUDA(cudaStreamSynchronize(st));
-        err = s->counters_host[0];
-        if (err) throw NrError(NR_ERR_DEVICE, "traversal error bits " + std::to_string(err) + " (1 stack overflow, 2 step cap)");
+        with_oom_release(s, [&]() {
+            NR_CUDA(cudaSetDevice(s->device));
+            ensure_paths(s, 1);
+            cudaStream_t st = s->stream;
+            const float *dO = o, *dD = d;
+            int32_t* dTri = tri;
+            float *dT = t, *dB1 = b1, *dB2 = b2;
+            if (!(flags & NR_PTR_DEVICE)) {
+                size_t f3 = (size_t)n * 12, f1 = (size_t)n * 4;
+                s->scratch.ensure(2 * f3 + 4 * f1 + 6 * 256);  // six 256-byte aligned pieces
+                char* p = s->scratch.as<char>();
+                auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
+                float* xo = (float*)take(f3);
+                float* xd = (float*)take(f3);
+                dTri = (int32_t*)take(f1); dT = (float*)take(f1); dB1 = (float*)take(f1); dB2 = (float*)take(f1);
+                NR_CUDA(cudaMemcpyAsync(xo, o, f3, cudaMemcpyHostToDevice, st));
+                NR_CUDA(cudaMemcpyAsync(xd, d, f3, cudaMemcpyHostToDevice, st));
+                dO = xo; dD = xd;
+            }
+            NR_CUDA(cudaMemsetAsync(s->ps.counters + nr::CNT_ERR, 0, 4, st));
+            nr::launch_intersect(scene_for(s, !(flags & NR_INTERSECT_EXHAUSTIVE)), n, dO, dD, dTri, dT, dB1, dB2,
+                                 s->ps.counters + nr::CNT_ERR, st);
+            NR_CUDA(cudaGetLastError());
+            if (!(flags & NR_PTR_DEVICE)) {
+                size_t f1 = (size_t)n * 4;
+                NR_CUDA(cudaMemcpyAsync(tri, dTri, f1, cudaMemcpyDeviceToHost, st));
+                NR_CUDA(cudaMemcpyAsync(t, dT, f1, cudaMemcpyDeviceToHost, st));
+                NR_CUDA(cudaMemcpyAsync(b1, dB1, f1, cudaMemcpyDeviceToHost, st));
+                NR_CUDA(cudaMemcpyAsync(b2, dB2, f1, cudaMemcpyDeviceToHost, st));
+            }
+            uint32_t err = 0;
+            NR_CUDA(cudaMemcpyAsync(s->counters_host, s->ps.counters + nr::CNT_ERR, 4, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+            err = s->counters_host[0];
+            if (err) throw NrError(NR_ERR_DEVICE, "traversal error bits " + std::to_string(err) + " (" + nr::err_bits_text() + ")");
+        });
     });
 }
 
@@ -1142,42 +1267,47 @@ int nr_render(nr_scene* s, const nr_camera* cam, const char* params, float* hdr_
     return guarded([&]() {
         if (!s) throw NrError(NR_ERR_INVALID, "null scene");
         std::lock_guard<std::mutex> lk(s->mu);
-        NR_CUDA(cudaSetDevice(s->device));
-        RenderArgs A = parse_args(cam, params);
-        const int npix = A.pol.imgw * A.pol.imgh;
-        cudaStream_t st = s->stream;
-        s->film.ensure((size_t)npix * sizeof(float4));
-        bool fresh = false;
-        if (!A.accumulate || s->film_pixels != npix) {
-            NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
-            s->film_samples = 0;
-            s->film_pixels = npix;
-            fresh = true;
-        }
-        int first = A.sample0;
-        if (A.nrc_pre && fresh) {
-            // RendererNRC::render (src/renderer/renderernrc.cpp:231-246): one
-            // pass in which every path trains, added to the image like the
-            // others, while the mean still divides by spp (:268)
-            RenderArgs P = A;
-            P.spp = 1;
-            P.pol.coin = 0;
-            P.pol.force_train = 1;
-            run_waves(s, P, npix, nullptr, first, s->film.as<float4>(), nullptr, cancel, nullptr, nullptr);
-            ++first;
-        }
-        run_waves(s, A, npix, nullptr, first, s->film.as<float4>(), nullptr, cancel, progress, user);
-        s->film_samples += (uint64_t)A.spp;
-        if (hdr_rgb || rgb8) {
-            if (hdr_rgb) s->out_hdr.ensure((size_t)npix * 12);
-            if (rgb8) s->out_rgb8.ensure((size_t)npix * 3);
-            nr::launch_finish(s->film.as<float4>(), npix, 1.0f / (float)s->film_samples, hdr_rgb ? s->out_hdr.as<float>() : nullptr,
-                              rgb8 ? s->out_rgb8.as<uint8_t>() : nullptr, st);
-            if (hdr_rgb) NR_CUDA(cudaMemcpyAsync(hdr_rgb, s->out_hdr.p, (size_t)npix * 12, cudaMemcpyDeviceToHost, st));
-            if (rgb8) NR_CUDA(cudaMemcpyAsync(rgb8, s->out_rgb8.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, st));
-            NR_CUDA(cudaStreamSynchronize(st));
-        }
-        NR_CUDA(cudaGetLastError());
+        with_oom_release(s, [&]() {
+            NR_CUDA(cudaSetDevice(s->device));
+            RenderArgs A = parse_args(cam, params);
+            const int npix = A.pol.imgw * A.pol.imgh;
+            cudaStream_t st = s->stream;
+            if (s->film.bytes < (size_t)npix * sizeof(float4)) {
+                s->film_pixels = 0;  // a new film holds nothing to accumulate onto
+                s->film.ensure((size_t)npix * sizeof(float4));
+            }
+            bool fresh = false;
+            if (!A.accumulate || s->film_pixels != npix) {
+                NR_CUDA(cudaMemsetAsync(s->film.p, 0, (size_t)npix * sizeof(float4), st));
+                s->film_samples = 0;
+                s->film_pixels = npix;
+                fresh = true;
+            }
+            int first = A.sample0;
+            if (A.nrc_pre && fresh) {
+                // RendererNRC::render (src/renderer/renderernrc.cpp:231-246): one
+                // pass in which every path trains, added to the image like the
+                // others, while the mean still divides by spp (:268)
+                RenderArgs P = A;
+                P.spp = 1;
+                P.pol.coin = 0;
+                P.pol.force_train = 1;
+                run_waves(s, P, npix, nullptr, first, s->film.as<float4>(), nullptr, cancel, nullptr, nullptr);
+                ++first;
+            }
+            run_waves(s, A, npix, nullptr, first, s->film.as<float4>(), nullptr, cancel, progress, user);
+            s->film_samples += (uint64_t)A.spp;
+            if (hdr_rgb || rgb8) {
+                if (hdr_rgb) s->out_hdr.ensure((size_t)npix * 12);
+                if (rgb8) s->out_rgb8.ensure((size_t)npix * 3);
+                nr::launch_finish(s->film.as<float4>(), npix, 1.0f / (float)s->film_samples, hdr_rgb ? s->out_hdr.as<float>() : nullptr,
+                                  rgb8 ? s->out_rgb8.as<uint8_t>() : nullptr, st);
+                if (hdr_rgb) NR_CUDA(cudaMemcpyAsync(hdr_rgb, s->out_hdr.p, (size_t)npix * 12, cudaMemcpyDeviceToHost, st));
+                if (rgb8) NR_CUDA(cudaMemcpyAsync(rgb8, s->out_rgb8.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, st));
+                NR_CUDA(cudaStreamSynchronize(st));
+            }
+            NR_CUDA(cudaGetLastError());
+        });
     });
 }
 
@@ -1186,20 +1316,22 @@ int nr_render_samples(nr_scene* s, const nr_camera* cam, const char* params, int
     return guarded([&]() {
         if (!s || npix <= 0 || !pix_xy || spp <= 0 || !out || sample0 < 0) throw NrError(NR_ERR_INVALID, "bad argument");
         std::lock_guard<std::mutex> lk(s->mu);
-        NR_CUDA(cudaSetDevice(s->device));
-        RenderArgs A = parse_args(cam, params);
-        A.spp = spp;
-        for (int32_t i = 0; i < npix; ++i)
-            if (pix_xy[2 * i] < 0 || pix_xy[2 * i] >= A.pol.imgw || pix_xy[2 * i + 1] < 0 || pix_xy[2 * i + 1] >= A.pol.imgh)
-                throw NrError(NR_ERR_INVALID, "pixel outside the image");
-        cudaStream_t st = s->stream;
-        size_t nout = (size_t)npix * spp * 3;
-        s->pix_list.ensure((size_t)npix * 8);
-        s->out_hdr.ensure(nout * 4);
-        NR_CUDA(cudaMemcpyAsync(s->pix_list.p, pix_xy, (size_t)npix * 8, cudaMemcpyHostToDevice, st));
-        run_waves(s, A, npix, s->pix_list.as<int32_t>(), sample0, nullptr, s->out_hdr.as<float>(), nullptr, nullptr, nullptr);
-        NR_CUDA(cudaMemcpyAsync(out, s->out_hdr.p, nout * 4, cudaMemcpyDeviceToHost, st));
-        NR_CUDA(cudaStreamSynchronize(st));
+        with_oom_release(s, [&]() {
+            NR_CUDA(cudaSetDevice(s->device));
+            RenderArgs A = parse_args(cam, params);
+            A.spp = spp;
+            for (int32_t i = 0; i < npix; ++i)
+                if (pix_xy[2 * i] < 0 || pix_xy[2 * i] >= A.pol.imgw || pix_xy[2 * i + 1] < 0 || pix_xy[2 * i + 1] >= A.pol.imgh)
+                    throw NrError(NR_ERR_INVALID, "pixel outside the image");
+            cudaStream_t st = s->stream;
+            size_t nout = (size_t)npix * spp * 3;
+            s->pix_list.ensure((size_t)npix * 8);
+            s->out_hdr.ensure(nout * 4);
+            NR_CUDA(cudaMemcpyAsync(s->pix_list.p, pix_xy, (size_t)npix * 8, cudaMemcpyHostToDevice, st));
+            run_waves(s, A, npix, s->pix_list.as<int32_t>(), sample0, nullptr, s->out_hdr.as<float>(), nullptr, nullptr, nullptr);
+            NR_CUDA(cudaMemcpyAsync(out, s->out_hdr.p, nout * 4, cudaMemcpyDeviceToHost, st));
+            NR_CUDA(cudaStreamSynchronize(st));
+        });
     });
 }
 
@@ -1235,6 +1367,16 @@ int nr_nrc_create(const char* params, nr_nrc** out) {
         n->ema = c.get_float("ema", 0.99f);
         if (n->ema < 0.f || n->ema >= 1.f) throw NrError(NR_ERR_INVALID, "ema must be in [0, 1)");
         n->tc = c.get_int("tc", 1) != 0;
+        // polls of the first bounded wait for a group of tensor-core MMAs;
+        // 0 makes every such wait time out at once (the timeout path: error
+        // bit 8, a second bounded wait for the MMAs in flight, tensor memory
+        // freed, NR_ERR_DEVICE)
+        {
+            const long long fw = c.get_int("tc_first_wait", (int)NR_TC_FIRST_WAIT_LIMIT);
+            if (fw < 0 || fw > (long long)NR_TC_FIRST_WAIT_LIMIT)
+                throw NrError(NR_ERR_INVALID, "tc_first_wait must be in [0, " + std::to_string(NR_TC_FIRST_WAIT_LIMIT) + "]");
+            n->tc_first_wait = (uint32_t)fw;
+        }
         nr::nrc_setup();
         nr::nrc_tc_setup();
         n->errbuf.alloc(256);
@@ -1306,7 +1448,94 @@ int nr_nrc_set_params(nr_nrc* n, const float* in) {
     });
 }
 
+// Optimizer state of a cache, for checkpoints: which = NR_NRC_STATE_*.
+int nr_nrc_get_state(nr_nrc* n, int32_t which, float* out) {
+    return guarded([&]() {
+        if (!n || !out) throw NrError(NR_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(n->mu);
+        NR_CUDA(cudaSetDevice(n->device));
+        const size_t P = NRC_NUM_PARAMS;
+        if (which == NR_NRC_STATE_STEP) {
+            out[0] = (float)n->step;
+            return;
+        }
+        float* src = nullptr;
+        const __nv_bfloat16* bsrc = nullptr;
+        switch (which) {
+            case NR_NRC_STATE_PARAMS: src = n->dev.params; break;
+            case NR_NRC_STATE_GRAD: src = n->dev.grad; break;
+            case NR_NRC_STATE_M: src = n->dev.m; break;
+            case NR_NRC_STATE_V: src = n->dev.v; break;
+            case NR_NRC_STATE_EMA: src = n->dev.ema; break;
+            case NR_NRC_STATE_INFER: src = n->dev.pinf; break;
+            case NR_NRC_STATE_PARAMS_BF16: bsrc = n->dev.wb; break;
+            case NR_NRC_STATE_INFER_BF16: bsrc = n->dev.wb_inf; break;
+            default: throw NrError(NR_ERR_INVALID, "unknown cache state " + std::to_string(which));
+        }
+        if (src) {
+            NR_CUDA(cudaMemcpyAsync(out, src, P * 4, cudaMemcpyDeviceToHost, n->stream));
+            NR_CUDA(cudaStreamSynchronize(n->stream));
+        } else {
+            std::vector<__nv_bfloat16> h(P);
+            NR_CUDA(cudaMemcpyAsync(h.data(), bsrc, P * 2, cudaMemcpyDeviceToHost, n->stream));
+            NR_CUDA(cudaStreamSynchronize(n->stream));
+            for (size_t i = 0; i < P; ++i) {
+                uint16_t b;
+                std::memcpy(&b, &h[i], 2);
+                const uint32_t u = (uint32_t)b << 16;
+                std::memcpy(&out[i], &u, 4);
+            }
+        }
+    });
+}
+
+int nr_nrc_set_state(nr_nrc* n, int32_t which, const float* in) {
+    return guarded([&]() {
+        if (!n || !in) throw NrError(NR_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(n->mu);
+        NR_CUDA(cudaSetDevice(n->device));
+        const size_t P = NRC_NUM_PARAMS;
+        if (which == NR_NRC_STATE_STEP) {
+            if (!(in[0] >= 0.f) || in[0] > 1e9f || in[0] != std::floor(in[0]))
+                throw NrError(NR_ERR_INVALID, "the step count must be a non-negative integer");
+            n->step = (int)in[0];
+            return;
+        }
+        float* dst = nullptr;
+        switch (which) {
+            case NR_NRC_STATE_PARAMS: dst = n->dev.params; break;
+            case NR_NRC_STATE_GRAD: dst = n->dev.grad; break;
+            case NR_NRC_STATE_M: dst = n->dev.m; break;
+            case NR_NRC_STATE_V: dst = n->dev.v; break;
+            case NR_NRC_STATE_EMA: dst = n->dev.ema; break;
+            case NR_NRC_STATE_INFER: dst = n->dev.pinf; break;
+            default: throw NrError(NR_ERR_INVALID, "cache state " + std::to_string(which) + " cannot be set");
+        }
+        NR_CUDA(cudaMemcpyAsync(dst, in, P * 4, cudaMemcpyHostToDevice, n->stream));
+        // the BF16 copies the kernels read follow their FP32 sources
+        if (which == NR_NRC_STATE_PARAMS) nr::nrc_launch_to_bf16(n->dev.params, n->dev.wb, P, n->stream);
+        if (which == NR_NRC_STATE_INFER) nr::nrc_launch_to_bf16(n->dev.pinf, n->dev.wb_inf, P, n->stream);
+        NR_CUDA(cudaStreamSynchronize(n->stream));
+        NR_CUDA(cudaGetLastError());
+    });
+}
+
 namespace {
+// Reads the cache's error word (already copied to err_host): clears it on
+// the device for the next call and turns a set bit into NR_ERR_DEVICE; bit
+// 32 also stops the process's use of the tensor-core kernels.
+void nrc_check_err(nr_nrc* c, const char* what) {
+    const uint32_t e = *c->err_host;
+    if (!e) return;
+    if (e & nr::NR_ERRBIT_TC_LOST) nr::nrc_tc_disable();
+    // the failed step's update was skipped; its partial gradient goes too
+    NR_CUDA(cudaMemsetAsync(c->dev.grad, 0, NRC_NUM_PARAMS * 4, c->stream));
+    NR_CUDA(cudaMemsetAsync(c->errbuf.p, 0, 4, c->stream));
+    NR_CUDA(cudaStreamSynchronize(c->stream));
+    throw NrError(NR_ERR_DEVICE, std::string("tensor-core ") + what + " wait timed out (error bits " + std::to_string(e) +
+                                     ": " + nr::err_bits_text() + ")");
+}
+
 // Uploads n rows of FP32 inputs and converts them to BF16 in the batch scratch.
 void nrc_upload_x(nr_nrc* c, int n, const float* x) {
     nrc_ensure_batch(c, n);
@@ -1322,16 +1551,16 @@ int nr_nrc_infer(nr_nrc* c, int32_t n, const float* x, float* out) {
         std::lock_guard<std::mutex> lk(c->mu);
         NR_CUDA(cudaSetDevice(c->device));
         nrc_upload_x(c, n, x);
-        if (c->tc)
+        if (c->use_tc())
             nr::nrc_launch_forward_tc(c->dev.wb, c->dev.params, c->x, nr::nrc_rows(n), c->out, c->num_sms,
-                                      c->errbuf.as<uint32_t>(), c->stream);
+                                      c->errbuf.as<uint32_t>(), c->stream, nullptr, c->tc_first_wait);
         else
             nr::nrc_launch_forward(c->dev, c->x, nr::nrc_rows(n), c->out, nullptr, c->num_sms, c->stream);
         NR_CUDA(cudaMemcpyAsync(out, c->out, (size_t)n * 12, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaMemcpyAsync(c->err_host, c->errbuf.p, 4, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaStreamSynchronize(c->stream));
         NR_CUDA(cudaGetLastError());
-        if (*c->err_host) throw NrError(NR_ERR_DEVICE, "tensor-core inference wait timed out");
+        nrc_check_err(c, "inference");
     });
 }
 
@@ -1346,7 +1575,8 @@ static int nrc_grad_impl(nr_nrc* c, int32_t n, const float* x, const float* y, f
         if (grad) NR_CUDA(cudaMemcpyAsync(grad, c->dev.grad, NRC_NUM_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream));
         if (update) {
             c->step++;
-            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, nr::nrc_rows(n), c->stream);
+            nr::nrc_launch_adam(c->dev, c->lr, c->b1, c->b2, c->eps, c->step, c->ema, nr::nrc_rows(n), c->stream,
+                                c->errbuf.as<uint32_t>());
         } else {
             NR_CUDA(cudaMemsetAsync(c->dev.grad, 0, NRC_NUM_PARAMS * 4, c->stream));
         }
@@ -1354,7 +1584,7 @@ static int nrc_grad_impl(nr_nrc* c, int32_t n, const float* x, const float* y, f
         NR_CUDA(cudaMemcpyAsync(c->err_host, c->errbuf.p, 4, cudaMemcpyDeviceToHost, c->stream));
         NR_CUDA(cudaStreamSynchronize(c->stream));
         NR_CUDA(cudaGetLastError());
-        if (*c->err_host) throw NrError(NR_ERR_DEVICE, "tensor-core training wait timed out");
+        nrc_check_err(c, "training");
         if (loss) *loss = *c->loss_host;
     });
 }

@@ -113,10 +113,16 @@ std::string scene_from_desc(const nr_scene_desc& d, HostScene& s) {
     if (d.nrm) s.nrm.assign(d.nrm, d.nrm + 9 * n);
     s.mat.assign(d.mat, d.mat + n);
     s.mats.assign(d.mats, d.mats + d.num_mats);
+    // NaN or infinite inputs are refused: the reference would carry them
+    // into every box and radiance they touch (it checks nothing)
     for (size_t i = 0; i < n; ++i) {
         if (s.mat[i] < 0 || s.mat[i] >= d.num_mats) return "triangle " + std::to_string(i) + ": material index out of range";
         for (int k = 0; k < 9; ++k)
             if (!std::isfinite(s.pos[9 * i + k])) return "triangle " + std::to_string(i) + ": non-finite position";
+        for (int k = 0; k < 9; ++k)
+            if (!std::isfinite(s.nrm[9 * i + k])) return "triangle " + std::to_string(i) + ": non-finite normal";
+        for (int k = 0; k < 6; ++k)
+            if (!std::isfinite(s.uv[6 * i + k])) return "triangle " + std::to_string(i) + ": non-finite texture coordinate";
     }
     size_t texels = 0;
     if (d.num_tex > 0) {
@@ -127,13 +133,19 @@ std::string scene_from_desc(const nr_scene_desc& d, HostScene& s) {
             texels += (size_t)s.tex_wh[2 * t] * s.tex_wh[2 * t + 1];
         }
         s.tex_data.assign(d.tex_data, d.tex_data + 3 * texels);
+        for (size_t i = 0; i < s.tex_data.size(); ++i)
+            if (!std::isfinite(s.tex_data[i])) return "texel value " + std::to_string(i) + " is not finite";
     }
     for (int m = 0; m < d.num_mats; ++m) {
         const nr_material& M = s.mats[m];
         if (M.type < NR_MAT_LAMBERT || M.type > NR_MAT_LIGHT) return "material " + std::to_string(m) + ": bad type";
         if (M.tex0 >= d.num_tex || M.tex1 >= d.num_tex) return "material " + std::to_string(m) + ": texture index out of range";
+        const float f[9] = {M.c0[0], M.c0[1], M.c0[2], M.c1[0], M.c1[1], M.c1[2], M.alpha, M.ior, M.ns};
+        for (float x : f)
+            if (!std::isfinite(x)) return "material " + std::to_string(m) + ": non-finite parameter";
     }
     if (d.env_tex >= d.num_tex) return "env_tex out of range";
+    if (!std::isfinite(d.env_gain)) return "env_gain is not finite";
     s.env_tex = d.env_tex < 0 ? -1 : d.env_tex;
     s.env_gain = d.env_gain;
     for (size_t i = 0; i < n; ++i) face_normal_rule(s, (int)i);

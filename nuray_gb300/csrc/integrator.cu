@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(128, 4) k_tail(PathState P, DeviceScene S, Pol
         P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
         if (!shade_one<NRC, -1, true>(P, S, pol, slot, C)) return;
     }
-    atomicOr(&P.counters[CNT_ERR], 2u);  // step cap: the path did not end
+    atomicOr(&P.counters[CNT_ERR], 16u);  // bounce cap: the path did not end
 }
 
 // ---------------------------------------------------------------- shadow rays

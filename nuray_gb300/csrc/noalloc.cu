@@ -7,8 +7,12 @@
 // account for every later allocation, or real-time loops that cannot afford
 // cudaMalloc's implicit device synchronisation in the middle of a frame.
 // For them this entry point stages through one file-scope device array of
-// fixed size, reserved when the library is loaded, and calls no cudaMalloc,
-// cudaFree or allocating library routine.
+// fixed size and calls no cudaMalloc, cudaFree or allocating library
+// routine. Under CUDA's lazy module loading the array is reserved on a
+// device when the module holding it is first loaded there; the library
+// does that, and looks up the array's address, when the first scene is
+// created on the device (noalloc_prepare), so the calls themselves load
+// and allocate nothing.
 #include <mutex>
 
 #include "nr_device.cuh"
@@ -28,6 +32,8 @@ constexpr size_t kOff_b1 = kOff_t + (size_t)NR_NOALLOC_MAX_RAYS * 4;
 constexpr size_t kOff_b2 = kOff_b1 + (size_t)NR_NOALLOC_MAX_RAYS * 4;
 constexpr size_t kOff_err = kOff_b2 + (size_t)NR_NOALLOC_MAX_RAYS * 4;
 constexpr size_t kScratchBytes = kOff_err + 256;  // 2.6 MB with 65,536 rays
+static_assert(kScratchBytes == (size_t)NR_NOALLOC_MAX_RAYS * 40 + 256,
+              "the static scratch is sized by include/nuray.h's NR_NOALLOC_MAX_RAYS");
 
 // Held by every device that loads the library until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -51,7 +57,27 @@ __global__ void k_intersect_noalloc(DeviceScene S, int n, const float* __restric
     b2[i] = v;
 }
 
+// Looks up (once per device, under g_mu) the device address of the scratch
+// on the current device, loading its module if lazy loading has not yet.
+std::string scratch_address(int device, char** out) {
+    if (device < 0 || device >= NR_NOALLOC_MAX_DEVICES) return "device index out of range for the static scratch";
+    if (!g_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+        g_addr[device] = p;
+    }
+    *out = static_cast<char*>(g_addr[device]);
+    return "";
+}
+
 }  // namespace
+
+std::string noalloc_prepare(int device) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    char* base = nullptr;
+    return scratch_address(device, &base);
+}
 
 std::string noalloc_intersect(const DeviceScene& S, int device, cudaStream_t st, int n, const float* o, const float* d,
                               int32_t* tri, float* t, float* b1, float* b2) {
@@ -63,13 +89,10 @@ std::string noalloc_intersect(const DeviceScene& S, int device, cudaStream_t st,
     if (n == 0) return "";
     // one call at a time: every call uses the same static array
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-        g_addr[device] = p;
-    }
-    char* base = static_cast<char*>(g_addr[device]);
+    // looked up when the scene was created; again here only if that failed
+    char* base = nullptr;
+    std::string err_addr = scratch_address(device, &base);
+    if (!err_addr.empty()) return err_addr;
     float* so = reinterpret_cast<float*>(base + kOff_o);
     float* sd = reinterpret_cast<float*>(base + kOff_d);
     int32_t* stri = reinterpret_cast<int32_t*>(base + kOff_tri);
@@ -95,7 +118,7 @@ std::string noalloc_intersect(const DeviceScene& S, int device, cudaStream_t st,
     if (e == cudaSuccess) e = cudaMemcpyAsync(&err, serr, 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return std::string("reading results: ") + cudaGetErrorString(e);
-    if (err) return "traversal error bits " + std::to_string(err) + " (1 stack overflow, 2 step cap)";
+    if (err) return "traversal error bits " + std::to_string(err) + " (" + err_bits_text() + ")";
     return "";
 }
 

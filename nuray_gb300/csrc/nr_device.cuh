@@ -231,11 +231,18 @@ __device__ __forceinline__ bool tri_test_fast(f3 o, f3 d, float4 g0, float4 g1, 
     return b1 >= 0.0f && b2 >= 0.0f && __fadd_rn(b1, b2) <= 1.0f;
 }
 
-// Pruning margin: a subtree whose entry distance exceeds the best hit by
-// more than this relative amount is skipped. The reference's biased
-// determinant (q + 1e-6) shortens t by a factor q / (q + 1e-6), so a
-// triangle can report a t slightly below its box's entry distance; the
-// margin keeps such triangles reachable unless |q| < 1e-6 / margin.
+// Pruning: a subtree whose entry distance exceeds the best hit so far (or a
+// shadow ray's limit) times S.prune_k is skipped; the reference prunes
+// nothing (src/hierarchy/bvh.cpp:116-117). The default factor is
+// 1 + NR_PRUNE_MARGIN. The reference's biased determinant (q + 1e-6,
+// src/scene/triangle.cpp:31) reports t' = t q / (q + 1e-6) and accepts the
+// triangle scaled about p0 by (q + 1e-6) / q, so a triangle crossed at a
+// grazing angle (0 < q < 1e-6 / margin, or |q| < 1e-6) can report a t
+// below its box's entry distance, even below the best hit of another
+// subtree; no bound from the boxes excludes it. Such rays need the plane
+// of a triangle to hold the ray to about 1e-6 of its length; prune=0
+// (S.prune_k = infinity) visits every node whose box the ray enters, as
+// the reference does, and returns the reference's hits for them too.
 // LightSampler::sampleLight (src/sampler/lightsampler.cpp:56): the first
 // emitter whose CDF entry is >= r (lower_bound), or the last one. The guide
 // table narrows the search to the emitters between the lower bounds of
@@ -252,7 +259,6 @@ __device__ __forceinline__ int pick_light(const DeviceScene& S, float r) {
     return lo < S.num_lights ? lo : S.num_lights - 1;
 }
 
-#define NR_PRUNE_MARGIN 1e-3f
 #define NR_STACK NR_STACK_LIMIT
 
 // Closest hit with the reference's exhaustive semantics (BVH::_traversal,
@@ -290,7 +296,7 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
             float t0, t1;
             bool h0 = FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
             bool h1 = FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
-            float lim = best_t * (1.0f + NR_PRUNE_MARGIN);
+            float lim = best_t * S.prune_k;
             h0 = h0 && t0 <= lim;
             h1 = h1 && t1 <= lim;
             if (h0 && h1) {
@@ -326,7 +332,7 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
         while (sp > 0) {
             --sp;
             const int2 e = stack[sp];
-            if (__int_as_float(e.y) <= best_t * (1.0f + NR_PRUNE_MARGIN)) { ref = e.x; found = true; break; }
+            if (__int_as_float(e.y) <= best_t * S.prune_k) { ref = e.x; found = true; break; }
         }
         if (!found) break;
     }
@@ -378,7 +384,7 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
         while (sp > 0) {
             --sp;
             const int2 e = stack[sp];
-            if (__int_as_float(e.y) <= best_t * (1.0f + NR_PRUNE_MARGIN)) return e.x;
+            if (__int_as_float(e.y) <= best_t * S.prune_k) return e.x;
         }
         return (int)NR_TRAV_END;
     };
@@ -392,7 +398,7 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
             float t0, t1;
             bool h0 = FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
             bool h1 = FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
-            const float lim = best_t * (1.0f + NR_PRUNE_MARGIN);
+            const float lim = best_t * S.prune_k;
             h0 = h0 && t0 <= lim;
             h1 = h1 && t1 <= lim;
             if (h0 && h1) {
@@ -466,7 +472,7 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
     SlabRay R = make_slab_ray(o, d);
     float te;
     if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return false;
-    const float lim = tmax * (1.0f + NR_PRUNE_MARGIN);
+    const float lim = tmax * S.prune_k;
     int stack[NR_STACK];
     int sp = 0;
     int ref = S.root_ref;
@@ -534,7 +540,7 @@ __device__ __forceinline__ bool any_hit(const DeviceScene& S, f3 o, f3 d, float 
     SlabRay R = make_slab_ray(o, d);
     float te;
     if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return false;
-    const float lim = tmax * (1.0f + NR_PRUNE_MARGIN);
+    const float lim = tmax * S.prune_k;
     int stack[NR_STACK];
     int sp = 0;
     int ref = S.root_ref;

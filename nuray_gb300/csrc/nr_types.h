@@ -10,6 +10,11 @@
 // rejected at creation.
 #define NR_STACK_LIMIT 96
 
+// Default pruning margin of the closest-hit and shadow walks: a subtree is
+// skipped when its entry distance exceeds the best hit by this relative
+// amount (DeviceScene::prune_k = 1 + NR_PRUNE_MARGIN; prune=0 turns it off).
+#define NR_PRUNE_MARGIN 1e-3f
+
 namespace nr {
 
 // BVH child reference: >= 0 is an internal node index, < 0 a leaf
@@ -61,6 +66,7 @@ struct DeviceScene {
     uint32_t cat_mask;        // shading categories that can occur: bit t for each material type present, and misses
     int32_t max_depth;        // deepest leaf (root = 0)
     int32_t num_nodes;        // internal nodes
+    float prune_k;            // subtrees entered beyond prune_k x the best hit are skipped (infinity: none)
 };
 
 // Render policy decoded from the parameter string.
@@ -143,7 +149,7 @@ enum Counter {
     CNT_WORK = 3,      // persistent-kernel work cursor (closest hit)
     CNT_WORK_SH = 4,   // persistent-kernel work cursor (shadow)
     CNT_CAT = 8,       // 8..14: per-category counts
-    CNT_ERR = 16,      // internal error bits: 1 stack overflow, 2 traversal step cap; 0 = fine
+    CNT_ERR = 16,      // internal error bits (NR_ERRBIT_*); 0 = fine
     CNT_RAYS = 18,     // 64-bit totals (lo, hi): extension rays,
     CNT_SHRAYS = 20,   // shadow rays,
     CNT_NODES = 22,    // BVH nodes visited by closest-hit rays (instrumented runs),
@@ -152,5 +158,23 @@ enum Counter {
     CNT_SH_TRIS = 28,  // triangles tested by shadow rays
     NUM_COUNTERS = 32
 };
+
+// Bits of counters[CNT_ERR], each set by a kernel that met the condition
+// and returned instead of going on; the host turns them into NR_ERR_DEVICE.
+enum ErrBit : uint32_t {
+    NR_ERRBIT_STACK = 1u,       // traversal stack overflow
+    NR_ERRBIT_STEPS = 2u,       // traversal step budget spent (corrupted tree)
+    NR_ERRBIT_SHADOW_Q = 4u,    // shadow-ray queue full
+    NR_ERRBIT_TC_WAIT = 8u,     // a tensor-core MMA wait timed out; the CTA waited again and stopped
+    NR_ERRBIT_BOUNCES = 16u,    // the tail kernel's path still alive after NR_TAIL_MAX_BOUNCES bounces
+    NR_ERRBIT_TC_LOST = 32u,    // the second MMA wait timed out too: tensor memory freed with MMAs possibly
+                                // in flight; the library stops using the tensor-core kernels
+};
+
+// Text for the error bits set in `bits`.
+inline const char* err_bits_text() {
+    return "1 stack overflow, 2 traversal step cap, 4 shadow queue full, 8 tensor-core wait timed out, "
+           "16 paths alive after 4096 bounces in the tail kernel, 32 tensor-core MMAs unfinished after a second wait";
+}
 
 }  // namespace nr

@@ -400,9 +400,10 @@ __global__ void __launch_bounds__(128) k_nrc_backward_weight(const __nv_bfloat16
 __global__ void k_nrc_adam(float* __restrict__ p, float* __restrict__ grad, float* __restrict__ m, float* __restrict__ v,
                            __nv_bfloat16* __restrict__ wb, float* __restrict__ ema, float* __restrict__ pinf,
                            __nv_bfloat16* __restrict__ wb_inf, int n, float lr, float b1, float b2, float eps, float c1,
-                           float c2, float beta, float cema, NrcRows R) {
+                           float c2, float beta, float cema, NrcRows R, const uint32_t* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (err && *err) return;  // a kernel of this step failed: its gradient is not applied
     int r0, rows;
     row_range(R, r0, rows);
     if (rows <= 0) return;  // an empty counted chunk: no step
@@ -474,11 +475,12 @@ void nrc_launch_backward_weight(const NrcDev& N, const __nv_bfloat16* x, const _
 }
 
 void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta,
-                     const NrcRows& R, cudaStream_t st) {
+                     const NrcRows& R, cudaStream_t st, const uint32_t* err) {
     float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
     float cema = 1.f - powf(ema_beta, (float)step);
     k_nrc_adam<<<(NRC_NUM_PARAMS + 255) / 256, 256, 0, st>>>(N.params, N.grad, N.m, N.v, N.wb, N.ema, N.pinf, N.wb_inf,
-                                                            NRC_NUM_PARAMS, lr, b1, b2, eps, c1, c2, ema_beta, cema, R);
+                                                            NRC_NUM_PARAMS, lr, b1, b2, eps, c1, c2, ema_beta, cema, R,
+                                                            err);
 }
 
 void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, const NrcRows& R, float* out, int num_sms,

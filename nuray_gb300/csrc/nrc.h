@@ -66,20 +66,36 @@ void nrc_launch_backward(const NrcDev& N, const __nv_bfloat16* x, const float* o
                          const __nv_bfloat16* acts, __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms,
                          cudaStream_t st);
 // ema_beta 0 keeps pinf / wb_inf equal to the current parameters. A counted
-// chunk without rows leaves the parameters unchanged.
+// chunk without rows leaves the parameters unchanged, and so does a nonzero
+// error word `err` (device, may be null): a kernel of the step failed.
 void nrc_launch_adam(const NrcDev& N, float lr, float b1, float b2, float eps, int step, float ema_beta,
-                     const NrcRows& R, cudaStream_t st);
+                     const NrcRows& R, cudaStream_t st, const uint32_t* err = nullptr);
 // Forward with the inference copy (pinf / wb_inf).
 void nrc_launch_forward_inf(const NrcDev& N, const __nv_bfloat16* x, const NrcRows& R, float* out, int num_sms,
                             cudaStream_t st);
 void nrc_launch_to_bf16(const float* a, __nv_bfloat16* b, size_t n, cudaStream_t st);
 
+// Polls of the tensor-core kernels' bounded mbarrier waits (about 40 ms of
+// polling on the GB300 before a wait counts as timed out).
+#ifndef NR_TC_FIRST_WAIT_LIMIT
+#define NR_TC_FIRST_WAIT_LIMIT (1u << 22)
+#endif
+
 // The forward on the tcgen05 tensor cores (nrc_tc.cu) with the BF16 weights
 // wb and the FP32 biases of params (either copy of a cache): out [rows][3].
-// err (device word) gets bit 8 when a tensor-core wait timed out.
+// err (device word) gets bit 8 when a tensor-core wait timed out (the CTA
+// then waits again, bounded, for the MMAs in flight, frees its tensor memory
+// and returns) and bit 32 as well when that second wait ran out too.
+// first_wait: the bound of the first wait of each layer.
 void nrc_tc_setup();
 void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
-                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts = nullptr);
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts = nullptr,
+                           uint32_t first_wait = NR_TC_FIRST_WAIT_LIMIT);
+// After error bit 32 the process stops launching the tensor-core kernels
+// (their tensor memory may have been freed under running MMAs): every cache
+// falls back to the mma.sync kernels of nrc.cu.
+void nrc_tc_disable();
+bool nrc_tc_enabled();
 // Training on the tensor cores: the data gradients (dz [5][ld][64], loss)
 // of k_nrc_backward_data by tcgen05.mma; the weight gradients then come
 // from nrc_launch_backward_weight.
@@ -87,7 +103,7 @@ void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const _
 // weights.
 void nrc_launch_backward_data_tc(const __nv_bfloat16* wb, const float* out, const float* y, const __nv_bfloat16* acts,
                                  __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms, void* wt_img,
-                                 uint32_t* err, cudaStream_t st);
+                                 uint32_t* err, cudaStream_t st, uint32_t first_wait = NR_TC_FIRST_WAIT_LIMIT);
 size_t nrc_wt_image_bytes();
 // The weight-gradient half of nrc_launch_backward (k_nrc_backward_weight).
 void nrc_launch_backward_weight(const NrcDev& N, const __nv_bfloat16* x, const __nv_bfloat16* dz,

@@ -19,7 +19,10 @@
 // memory and returns.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "nrc.h"
+#include "nr_types.h"
 
 namespace nr {
 
@@ -40,7 +43,11 @@ constexpr int SM_BIAS = SM_A + (TM / 8) * KC_IN * 128;
 constexpr int SM_BAR = SM_BIAS + (4 * H + 16) * 4;
 constexpr int SM_TOTAL = SM_BAR + 16;
 constexpr uint32_t TMEM_COLS = 64;
-constexpr uint32_t WAIT_LIMIT = 1u << 22;
+// Polls of one bounded mbarrier wait. The first wait of a layer takes the
+// caller's bound (NR_TC_FIRST_WAIT_LIMIT by default; a cache created with
+// tc_first_wait=0 makes it run out at once, which tests the timeout path);
+// the wait after a timeout, for the MMAs still in flight, always takes this one.
+constexpr uint32_t WAIT_LIMIT = NR_TC_FIRST_WAIT_LIMIT;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -65,8 +72,8 @@ __device__ __forceinline__ void commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
 }
 // Bounded wait for the mbarrier phase; false on timeout.
-__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t phase) {
-    for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t phase, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -122,7 +129,7 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
                                                         const float* __restrict__ params,
                                                         const __nv_bfloat16* __restrict__ x, NrcRows R,
                                                         float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
-                                                        uint32_t* err) {
+                                                        uint32_t* err, uint32_t first_wait) {
     int m0, M;
     if (!R.count) {
         m0 = 0;
@@ -206,14 +213,15 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
                 }
                 commit(bar);
             }
-            const bool ok = wait_phase(bar, phase);
+            const bool ok = wait_phase(bar, phase, first_wait);
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
-                    atomicOr(err, 8u);
                     s_abort = 1;
                     // the MMAs may still write the tensor memory freed below:
-                    // one more bounded wait for their commit
-                    wait_phase(bar, phase);
+                    // one more bounded wait for their commit; if that runs
+                    // out too, bit 32 tells the host to stop using these kernels
+                    const bool done = wait_phase(bar, phase, WAIT_LIMIT);
+                    atomicOr(err, done ? (uint32_t)NR_ERRBIT_TC_WAIT : (uint32_t)(NR_ERRBIT_TC_WAIT | NR_ERRBIT_TC_LOST));
                 }
                 break;
             }
@@ -308,7 +316,7 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data_tc(const __nv_bfloat1
                                                               const __nv_bfloat16* __restrict__ acts, NrcRows R,
                                                               __nv_bfloat16* __restrict__ dz, float* loss_sum,
                                                               const unsigned char* __restrict__ wt_img,
-                                                              uint32_t* err) {
+                                                              uint32_t* err, uint32_t first_wait) {
     int m0, M;
     if (!R.count) {
         m0 = 0;
@@ -391,14 +399,15 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data_tc(const __nv_bfloat1
                 }
                 commit(bar);
             }
-            const bool ok = wait_phase(bar, phase);
+            const bool ok = wait_phase(bar, phase, first_wait);
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
-                    atomicOr(err, 8u);
                     s_abort = 1;
                     // the MMAs may still write the tensor memory freed below:
-                    // one more bounded wait for their commit
-                    wait_phase(bar, phase);
+                    // one more bounded wait for their commit; if that runs
+                    // out too, bit 32 tells the host to stop using these kernels
+                    const bool done = wait_phase(bar, phase, WAIT_LIMIT);
+                    atomicOr(err, done ? (uint32_t)NR_ERRBIT_TC_WAIT : (uint32_t)(NR_ERRBIT_TC_WAIT | NR_ERRBIT_TC_LOST));
                 }
                 break;
             }
@@ -446,26 +455,33 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data_tc(const __nv_bfloat1
 
 size_t nrc_forward_tc_smem() { return (size_t)SM_TOTAL; }
 
+namespace {
+std::atomic<bool> g_tc_disabled{false};
+}
+void nrc_tc_disable() { g_tc_disabled.store(true); }
+bool nrc_tc_enabled() { return !g_tc_disabled.load(); }
+
 void nrc_tc_setup() {
     cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc_forward_tc_smem());
     cudaFuncSetAttribute(k_nrc_backward_data_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, BK_TOTAL);
 }
 
 void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
-                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts) {
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts,
+                           uint32_t first_wait) {
     const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
     if (M <= 0) return;
     int blocks = (M + TM - 1) / TM;
     const int cap = num_sms * 3;  // three resident CTAs per SM by shared memory (64 tensor-memory columns each)
     if (blocks > cap) blocks = cap;
-    k_nrc_forward_tc<<<blocks, 128, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, acts, err);
+    k_nrc_forward_tc<<<blocks, 128, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, acts, err, first_wait);
 }
 
 size_t nrc_wt_image_bytes() { return (size_t)BK_A; }
 
 void nrc_launch_backward_data_tc(const __nv_bfloat16* wb, const float* out, const float* y, const __nv_bfloat16* acts,
                                  __nv_bfloat16* dz, const NrcRows& R, float* loss_sum, int num_sms, void* wt_img,
-                                 uint32_t* err, cudaStream_t st) {
+                                 uint32_t* err, cudaStream_t st, uint32_t first_wait) {
     const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
     if (M <= 0) return;
     k_nrc_pack_wt<<<4, 256, 0, st>>>(wb, static_cast<unsigned char*>(wt_img));
@@ -473,7 +489,7 @@ void nrc_launch_backward_data_tc(const __nv_bfloat16* wb, const float* out, cons
     const int cap = num_sms * 4;  // 43 KB of shared memory and 64 tensor-memory columns per CTA
     if (blocks > cap) blocks = cap;
     k_nrc_backward_data_tc<<<blocks, 128, BK_TOTAL, st>>>(wb, out, y, acts, R, dz, loss_sum,
-                                                          static_cast<const unsigned char*>(wt_img), err);
+                                                          static_cast<const unsigned char*>(wt_img), err, first_wait);
 }
 
 }  // namespace nr

@@ -48,6 +48,23 @@ class Cache:
         assert p.size == NUM_PARAMS
         check(self.L.nr_nrc_set_params(self._h, _ptr(p)))
 
+    # nr_nrc_get_state / nr_nrc_set_state selectors
+    STATE = dict(params=0, grad=1, m=2, v=3, ema=4, infer=5, params_bf16=6, infer_bf16=7, step=8)
+
+    def get_state(self, which):
+        """One array of the training state (include/nuray.h NR_NRC_STATE_*);
+        'step' returns the Adam step count."""
+        k = self.STATE[which]
+        out = np.zeros(1 if which == "step" else NUM_PARAMS, np.float32)
+        check(self.L.nr_nrc_get_state(self._h, k, _ptr(out)))
+        return int(out[0]) if which == "step" else out
+
+    def set_state(self, which, value):
+        k = self.STATE[which]
+        a = np.array([value], np.float32) if which == "step" else np.ascontiguousarray(value, np.float32)
+        assert which == "step" or a.size == NUM_PARAMS
+        check(self.L.nr_nrc_set_state(self._h, k, _ptr(a)))
+
     def infer(self, x):
         x = np.ascontiguousarray(x, np.float32).reshape(-1, INPUTS)
         out = np.zeros((x.shape[0], 3), np.float32)

@@ -232,3 +232,92 @@ def test_tensor_core_training_gradient_equals_mma_sync(gpu_lib):
         cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
         rel = float(np.linalg.norm(a - b) / np.linalg.norm(b))
         assert cos > 0.999 and rel < 0.03, (k, cos, rel)
+
+
+def _bf16(a):
+    """float32 -> BF16 (round to nearest even) -> float32, as __float2bfloat16."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("tc", [1, 0])
+def test_adam_step_matches_numpy(gpu_lib, tc):
+    """One k_nrc_adam step against the same update in numpy (Kingma and Ba;
+    bias corrections 1 - beta^t at step t, the moving average
+    ema = b ema + (1 - b) p read as ema / (1 - b^t), and the BF16 copies of
+    both). The state is set through nr_nrc_set_state (parameters, gradient,
+    moments, moving average, step 4), then one nr_nrc_train_step runs on
+    rows whose targets are the cache's own predictions, so the loss gradient
+    is exactly zero and the step applies the set gradient alone.
+    Tolerances: each FP32 result within 4 ulp of the largest term that forms
+    it (the kernel may fuse a multiply and an add), the parameters within
+    1e-5 of their update on top; the BF16 copies are the round-to-nearest-
+    even of the kernel's own FP32 results."""
+    from nuray_gb300.nrc import NUM_PARAMS, Cache
+    lr, b1, b2, eps, beta = 2e-3, 0.9, 0.99, 1e-8, 0.95
+    c = Cache(f"seed=5 tc={tc} lr={lr} beta1={b1} beta2={b2} eps={eps} ema={beta}")
+    rng = np.random.default_rng(17)
+    p = (c.get_params() + rng.normal(scale=0.02, size=NUM_PARAMS)).astype(np.float32)
+    g = rng.normal(scale=1e-2, size=NUM_PARAMS).astype(np.float32)
+    g[::97] = 0.0
+    m = rng.normal(scale=1e-2, size=NUM_PARAMS).astype(np.float32)
+    v = rng.uniform(1e-6, 1e-4, size=NUM_PARAMS).astype(np.float32)
+    e = (p * rng.uniform(0.5, 1.0, size=NUM_PARAMS)).astype(np.float32)
+    for k, a in (("params", p), ("m", m), ("v", v), ("ema", e), ("step", 4)):
+        c.set_state(k, a)
+    x = rand_inputs(777, 3)
+    y = c.infer(x)  # the training forward reproduces these bits: a zero loss gradient
+    c.set_state("grad", g)
+    c.train_step(x, y)
+    assert c.get_state("step") == 5
+    t = 5
+    D = lambda a: np.asarray(a, np.float64)
+    c1, c2, ce = 1 - np.float32(b1) ** t, 1 - np.float32(b2) ** t, 1 - np.float32(beta) ** t
+    b1_, b2_, be_ = D(np.float32(b1)), D(np.float32(b2)), D(np.float32(beta))
+    m1 = b1_ * D(m) + (1 - b1_) * D(g)
+    v1 = b2_ * D(v) + (1 - b2_) * D(g) ** 2
+    upd = D(np.float32(lr)) * (m1 / c1) / (np.sqrt(v1 / c2) + eps)
+    p1 = D(p) - upd
+    e1 = be_ * D(e) + (1 - be_) * p1
+    q1 = e1 / ce
+    ulp = lambda a: np.spacing(np.abs(a).astype(np.float32)).astype(np.float64)
+    checks = (("m", m1, np.maximum(np.abs(b1_ * D(m)), np.abs((1 - b1_) * D(g))), 0),
+              ("v", v1, np.maximum(b2_ * D(v), (1 - b2_) * D(g) ** 2), 0),
+              ("params", p1, np.maximum(np.abs(D(p)), np.abs(upd)), 1e-5 * np.abs(upd)),
+              ("ema", e1, np.maximum(np.abs(be_ * D(e)), np.abs((1 - be_) * p1)), 1e-5 * np.abs(upd)),
+              ("infer", q1, np.abs(q1), 1e-5 * np.abs(upd) / ce))
+    for name, want, scale, extra in checks:
+        err = np.abs(D(c.get_state(name)) - want)
+        tol = 4 * ulp(scale) + extra + 1e-30
+        assert np.all(err <= tol), (name, float(np.max(err / tol)))
+    assert np.all(c.get_state("grad") == 0.0)  # cleared for the next accumulation
+    for name, src in (("params_bf16", "params"), ("infer_bf16", "infer")):
+        np.testing.assert_array_equal(c.get_state(name), _bf16(c.get_state(src)))
+
+
+def test_tensor_core_wait_timeout_path(gpu_lib):
+    """tc_first_wait=0 makes every first wait for a group of tcgen05 MMAs run
+    out at once: the CTA sets error bit 8, waits again (bounded) for the
+    MMAs it issued, frees its tensor memory and returns, and the call fails
+    with NR_ERR_DEVICE. Bit 32 (that second wait ran out too) must not be
+    set. Afterwards the same context still computes correctly: a cache with
+    the default bound gives the mma.sync kernels' outputs and gradients."""
+    from nuray_gb300 import NuRayError
+    from nuray_gb300.nrc import Cache
+    x = rand_inputs(1000, 5)
+    rng = np.random.default_rng(6)
+    y = rng.uniform(0, 2, size=(1000, 3)).astype(np.float32)
+    bad = Cache("seed=2 tc=1 tc_first_wait=0")
+    for call in (lambda: bad.infer(x), lambda: bad.gradient(x, y), lambda: bad.train_step(x, y)):
+        with pytest.raises(NuRayError, match=r"NR_ERR_DEVICE.*error bits 8:") as ei:
+            call()
+        assert "error bits 40" not in str(ei.value)
+    good, ref = Cache("seed=2 tc=1"), Cache("seed=2 tc=0")
+    np.testing.assert_allclose(good.infer(x), ref.infer(x), rtol=1e-2, atol=2e-3)
+    ga, la = good.gradient(x, y)
+    gb, lb = ref.gradient(x, y)
+    assert abs(la - lb) <= 1e-2 * abs(lb)
+    assert float(ga @ gb / (np.linalg.norm(ga) * np.linalg.norm(gb))) > 0.999
+    # the failed cache recovers too once its error word has been reported
+    assert np.all(np.isfinite(Cache("seed=2 tc=1").infer(x)))

@@ -247,3 +247,28 @@ def test_env_miss_and_textures_vs_port(gpu_lib, port_lib, renderer):
     a = S.render_samples(params, pix, 4)
     b = P.render_samples(params, pix, 4)
     assert _sample_match(a, b) >= 0.97
+
+
+def test_rgb8_vs_reference_render(gpu_lib, port_lib):
+    """nr_render's 8-bit output against the reference's own RendererPTLS::render
+    (src/renderer/rendererptls.cpp:165-181; fixture tests/golden/cornell_render_rgb8.npz,
+    the reference's frame loop run whole on the Philox stream) for the
+    Cornell workload, 320x240 at 16 spp. Where the GPU's per-pixel HDR mean
+    agrees with the CPU restatement's mean of the same samples (every
+    channel within the per-sample tolerance, rtol 2e-3 / atol 1e-4), the
+    8-bit values may differ by one level only (a mean within that tolerance
+    of a truncation boundary); at least 97 % of pixels agree that way, and
+    most are identical."""
+    g = golden("cornell_render_rgb8.npz")
+    params = str(g["params"])
+    S, P = gpu_scene(cornell_scene()), Oracle("port", cornell_scene())
+    hdr, rgb8 = S.render(params + f" seed={int(g['seed'])}", want_rgb8=True)
+    ref8 = g["rgb8"].astype(np.int32)
+    mean = P.render_samples(params, pixel_grid(320, 240), 16, seed=int(g["seed"])).astype(np.float64).mean(1)
+    agree = np.all(np.isclose(hdr.reshape(-1, 3).astype(np.float64), mean, rtol=2e-3, atol=1e-4), axis=1)
+    diff = np.abs(rgb8.astype(np.int32) - ref8).reshape(-1, 3).max(1)
+    print(f"8-bit vs the reference's render(): {np.mean(diff == 0) * 100:.2f}% identical, "
+          f"{np.mean(diff <= 1) * 100:.2f}% within one level; HDR agrees on {agree.mean() * 100:.2f}%")
+    assert np.all(diff[agree] <= 1)
+    assert agree.mean() >= 0.97
+    assert np.mean(diff == 0) >= 0.95

@@ -9,14 +9,22 @@ since the array keeps the previous call's contents.
 Named to be collected last, so a run that stops at the first failure has
 already run every other test; it also passes on its own in a fresh process.
 """
-import ctypes
+import os
+import re
 
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import ROOT, golden
 
 pytestmark = pytest.mark.gpu
+
+
+def _max_rays():
+    """NR_NOALLOC_MAX_RAYS as the public header defines it (the library's
+    limit and its array size come from the same definition)."""
+    text = open(os.path.join(ROOT, "include", "nuray.h")).read()
+    return int(re.search(r"#define NR_NOALLOC_MAX_RAYS (\d+)", text).group(1))
 
 
 def _scene():
@@ -58,12 +66,13 @@ def test_noalloc_rejects_batches_over_the_limit(gpu_lib):
     from nuray_gb300 import NuRayError
     from nuray_gb300._lib import _ptr, check, lib
     S = _scene()
-    n = 65536 + 1
+    limit = _max_rays()
+    n = limit + 1
     o = np.zeros((n, 3), np.float32)
     d = np.tile(np.array([0, 0, -1], np.float32), (n, 1))
     out = [np.zeros(n, np.int32)] + [np.zeros(n, np.float32) for _ in range(3)]
-    with pytest.raises(NuRayError, match="at most 65536 rays"):
+    with pytest.raises(NuRayError, match=f"at most {limit} rays"):
         check(lib().nr_intersect_noalloc(S._h, n, _ptr(o), _ptr(d), *[_ptr(a) for a in out]))
     # the full limit is accepted
-    tri, t, _, _ = _noalloc(S, o[:65536], d[:65536])
-    assert tri.shape == (65536,)
+    tri, t, _, _ = _noalloc(S, o[:limit], d[:limit])
+    assert tri.shape == (limit,)
