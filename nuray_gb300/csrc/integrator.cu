@@ -121,12 +121,22 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 #ifndef NR_WW
 #define NR_WW 5
 #endif
+// Entries of each traversal stack kept in shared memory (a power of two; 0:
+// all in local memory). Measured on the 1M-triangle frame: see DESIGN.
+#ifndef NR_SMEM_STACK
+#define NR_SMEM_STACK 0
+#endif
 
 template <bool COUNT, bool FAST>
 __global__ void __launch_bounds__(128, NR_TRACE_MINB) k_trace(PathState P, DeviceScene S, int capacity) {
     const uint32_t n = P.counters[CNT_IN];
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
+#if NR_SMEM_STACK
+    __shared__ int2 ring[NR_SMEM_STACK * 128];
+#else
+    int2* ring = nullptr;
+#endif
     while (true) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK], 32u);
@@ -137,8 +147,9 @@ __global__ void __launch_bounds__(128, NR_TRACE_MINB) k_trace(PathState P, Devic
             int slot = P.queue_in[idx];
             f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
             float t, b1, b2;
-            int tri = (NR_WW & 9) ? closest_hit_ww<FAST, (NR_WW & 1) != 0>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
-                                                   COUNT ? &nt : nullptr)
+            int tri = (NR_WW & 9) ? closest_hit_ww<FAST, (NR_WW & 1) != 0, NR_SMEM_STACK>(
+                                        S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                        COUNT ? &nt : nullptr, ring)
                             : closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
                                                 COUNT ? &nt : nullptr);
             P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
@@ -176,6 +187,11 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
     const uint32_t n = min(P.counters[CNT_SHADOW], (uint32_t)P.sh_cap);
     const int lane = threadIdx.x & 31;
     uint32_t nv = 0, nt = 0;
+#if NR_SMEM_STACK
+    __shared__ int ring[NR_SMEM_STACK * 128];
+#else
+    int* ring = nullptr;
+#endif
     while (true) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&P.counters[CNT_WORK_SH], 32u);
@@ -187,8 +203,9 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
             const bool env = o.w < 0.f;  // an environment sample: k_env_fold adds it
             const float tmax = env ? -o.w : o.w;
             const bool occluded =
-                (NR_WW & 6) ? any_hit_ww<FAST, (NR_WW & 2) != 0>(S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
-                                         COUNT ? &nt : nullptr)
+                (NR_WW & 6) ? any_hit_ww<FAST, (NR_WW & 2) != 0, NR_SMEM_STACK>(
+                                  S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
+                                  COUNT ? &nt : nullptr, ring)
                       : any_hit<FAST>(S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
                                       COUNT ? &nt : nullptr);
             if (P.vis) P.vis[__float_as_int(d.w)] = occluded ? 0 : 1;

@@ -7,6 +7,12 @@
 
 #include "nr_types.h"
 
+// Build-time switch for measurements: 1 takes the one-FMA slab test's
+// answer without its error margin and exact fallback.
+#ifndef NR_BOX_PLAIN
+#define NR_BOX_PLAIN 0
+#endif
+
 namespace nr {
 
 // ------------------------------------------------------------------ vectors
@@ -158,6 +164,10 @@ __device__ __forceinline__ bool box_test_fast(const SlabRay& r, float lx, float 
     float z1 = __fmaf_rn(lz, r.rz, r.cz), z2 = __fmaf_rn(hz, r.rz, r.cz);
     float tin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fmaxf(fminf(z1, z2), -1e18f));
     float tout = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fminf(fmaxf(z1, z2), 1e18f));
+#if NR_BOX_PLAIN
+    t_entry = tin;
+    return tin <= tout && tout >= 0.0f;
+#endif
     float margin = 1e-6f * fmaxf(fabsf(tin), fabsf(tout)) + r.abs_err;
     if (tout < -margin) return false;
     if (tin + margin < tout && tout > margin) { t_entry = tin; return true; }
@@ -363,27 +373,56 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
 // Refs: inner nodes >= 0, leaves < 0; NR_TRAV_END (no node) ends the walk.
 #define NR_TRAV_END 0x7fffffff
 
-template <bool FAST, bool SPEC = true>
+// Traversal stacks. The default keeps every entry in per-thread local
+// memory (L1-resident). With K > 0 the top K entries of each thread live in
+// a shared-memory ring (entry i at ring[(i % K) * blockDim.x]: threads of a
+// warp in adjacent banks) and only deeper entries go to local memory, moved
+// there when the ring is full and back when it drains.
+template <class E, int K>
+struct TravStack {
+    E spill[NR_STACK];
+    E* ring;  // this thread's column of the block's ring, or null
+    int sp = 0;
+    __device__ __forceinline__ void init(E* block_ring) { ring = block_ring ? block_ring + threadIdx.x : nullptr; }
+    __device__ __forceinline__ bool full() const { return sp >= NR_STACK; }
+    __device__ __forceinline__ bool empty() const { return sp == 0; }
+    __device__ __forceinline__ void push(E e) {
+        if (K == 0) { spill[sp++] = e; return; }
+        E* slot = ring + (sp & (K - 1)) * blockDim.x;
+        if (sp >= K) spill[sp - K] = *slot;  // the entry K below the top leaves the ring
+        *slot = e;
+        ++sp;
+    }
+    __device__ __forceinline__ E pop() {
+        --sp;
+        if (K == 0) return spill[sp];
+        E* slot = ring + (sp & (K - 1)) * blockDim.x;
+        const E e = *slot;
+        if (sp >= K) *slot = spill[sp - K];  // the entry K below comes back into the ring
+        return e;
+    }
+};
+
+template <bool FAST, bool SPEC = true, int K = 0>
 __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, float& best_t, float& best_b1,
                                               float& best_b2, uint32_t* err, uint32_t* nodes_visited = nullptr,
-                                              uint32_t* tris_tested = nullptr) {
+                                              uint32_t* tris_tested = nullptr, int2* ring = nullptr) {
     best_t = 1e18f; best_b1 = 0.f; best_b2 = 0.f;
     int best = -1, best_leaf = -1;
     if (S.root_ref == INT32_MIN) return -1;
     SlabRay R = make_slab_ray(o, d);
     float te;
     if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return -1;
-    int2 stack[NR_STACK];
-    int sp = 0;
+    TravStack<int2, K> stack;
+    stack.init(ring);
     int ref = S.root_ref;
     int leaf = 0;  // postponed leaf (< 0), or none (>= 0)
     uint32_t nv = 0, nt = 0;
     int budget = 2 * S.num_nodes + 8;
     // the next stacked subtree that can still hold a hit, or NR_TRAV_END
     auto pop = [&]() {
-        while (sp > 0) {
-            --sp;
-            const int2 e = stack[sp];
+        while (!stack.empty()) {
+            const int2 e = stack.pop();
             if (__int_as_float(e.y) <= best_t * S.prune_k) return e.x;
         }
         return (int)NR_TRAV_END;
@@ -405,8 +444,8 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
                 int nr = k.x, fr = k.y;
                 float ft = t1;
                 if (t1 < t0) { nr = k.y; fr = k.x; ft = t0; }
-                if (sp >= NR_STACK) { atomicOr(err, 1u); ref = NR_TRAV_END; leaf = 0; break; }
-                stack[sp] = make_int2(fr, __float_as_int(ft)); ++sp;
+                if (stack.full()) { atomicOr(err, 1u); ref = NR_TRAV_END; leaf = 0; break; }
+                stack.push(make_int2(fr, __float_as_int(ft)));
                 ref = nr;
             } else if (h0) {
                 ref = k.x;
@@ -465,16 +504,17 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
 
 // Any hit with t <= tmax, traversed as closest_hit_ww (SPEC), or while-while
 // without postponing: a lane's inner-node loop ends at its first leaf.
-template <bool FAST, bool SPEC>
+template <bool FAST, bool SPEC, int K = 0>
 __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, float tmax, uint32_t* err,
-                                           uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr) {
+                                           uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr,
+                                           int* ring = nullptr) {
     if (S.root_ref == INT32_MIN) return false;
     SlabRay R = make_slab_ray(o, d);
     float te;
     if (!box_test(R, S.root_lo[0], S.root_hi[0], S.root_lo[1], S.root_hi[1], S.root_lo[2], S.root_hi[2], te)) return false;
     const float lim = tmax * S.prune_k;
-    int stack[NR_STACK];
-    int sp = 0;
+    TravStack<int, K> stack;
+    stack.init(ring);
     int ref = S.root_ref;
     int leaf = 0;
     const float limit = fminf(1e18f, __uint_as_float(__float_as_uint(tmax) + 1u));  // accepts t <= tmax
@@ -495,27 +535,27 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
                 // ray leaves and its neighbours, which seldom occlude it
                 // (1M-triangle frame: 722.5 Mpaths/s near first, 759.8 far first)
                 if (t1 > t0) { nr = k.y; fr = k.x; }
-                if (sp >= NR_STACK) { atomicOr(err, 1u); return false; }
-                stack[sp++] = fr;
+                if (stack.full()) { atomicOr(err, 1u); return false; }
+                stack.push(fr);
                 ref = nr;
             } else if (h0) {
                 ref = k.x;
             } else if (h1) {
                 ref = k.y;
             } else {
-                ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+                ref = stack.empty() ? NR_TRAV_END : stack.pop();
             }
             if (SPEC) {
                 if (ref < 0 && leaf >= 0) {
                     leaf = ref;
-                    ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+                    ref = stack.empty() ? NR_TRAV_END : stack.pop();
                 }
                 if (!__any_sync(__activemask(), leaf >= 0)) break;
             }
         }
         if (!SPEC && ref < 0) {  // the leaf reached: tested at once
             leaf = ref;
-            ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+            ref = stack.empty() ? NR_TRAV_END : stack.pop();
         }
         while (leaf < 0) {
             int first = leaf_first(leaf), cnt = leaf_count(leaf);
@@ -527,7 +567,7 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
                 if (FAST ? tri_test_fast(o, d, g0, g1, g2, limit, t, u, v) : tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
             }
             leaf = ref;
-            if (ref < 0) ref = sp > 0 ? stack[--sp] : NR_TRAV_END;
+            if (ref < 0) ref = stack.empty() ? NR_TRAV_END : stack.pop();
         }
     }
     return false;
