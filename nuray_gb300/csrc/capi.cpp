@@ -145,7 +145,7 @@ struct nr_scene {
     nr::HostScene host;
     nr::Bvh bvh;
     nr::DeviceScene dev{};
-    DevBuf nodes, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_guide, light_mat;
+    DevBuf nodes, nodes_fast, tri_geo, tri_shade, mats, texels, tex_info, lights, light_cdf, light_guide, light_mat;
     DevBuf adj_L;  // per-path radiance for the adjoint replay
     DevBuf adj_wave;  // per-slot state of the wavefront adjoint replay
     DevBuf env_weight, env_row_cdf, env_col_cdf;  // environment sampling table (envis=1)
@@ -173,7 +173,8 @@ struct nr_scene {
         for (auto* b : all_bufs()) b->budget = &budget;
     }
     std::vector<DevBuf*> all_bufs() {
-        return {&nodes, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_guide, &light_mat,
+        return {&nodes, &nodes_fast, &tri_geo, &tri_shade, &mats, &texels, &tex_info, &lights, &light_cdf, &light_guide,
+                &light_mat,
                 &adj_L, &adj_wave, &env_weight, &env_row_cdf, &env_col_cdf, &path_mem, &film, &out_hdr, &out_rgb8,
                 &pix_list, &scratch, &nrc_mem};
     }
@@ -192,8 +193,8 @@ namespace {
 
 uint64_t device_bytes(const nr_scene* s) {
     uint64_t b = 0;
-    for (auto* x : {&s->nodes, &s->tri_geo, &s->tri_shade, &s->mats, &s->texels, &s->tex_info, &s->lights, &s->light_cdf,
-                    &s->light_guide, &s->light_mat})
+    for (auto* x : {&s->nodes, &s->nodes_fast, &s->tri_geo, &s->tri_shade, &s->mats, &s->texels, &s->tex_info, &s->lights,
+                    &s->light_cdf, &s->light_guide, &s->light_mat})
         b += x->bytes;
     return b;
 }
@@ -252,6 +253,30 @@ void upload_scene(nr_scene* s) {
         g.d = make_int4(ref_of(N.left), ref_of(N.right), N.depth, 0);
     }
     s->num_gpu_nodes = ng;
+
+    // The same nodes with every child box widened by delta for the one-FMA
+    // box test without margin (traversal mode 2). For a ray origin o with
+    // |o_i| <= Bo and box bounds b with |b_i| <= A, the test's quotient
+    // fma(b, 1/d, -o/d) and the reference's RN(RN(b - o) / d) each lie within
+    // 2^-23 (|b| + |o|) / |d| of (b - o) / d, so widening by more than
+    // 2.4e-7 (A + Bo) makes the test accept every box the reference's test
+    // accepts. Origins are allowed out to Bo = 2 A + 4 E (E the largest half
+    // extent of the scene box); delta = 4e-6 (A + E) covers that with more
+    // than 2x to spare, and is a relative 1e-3 of a 1M-triangle scene's
+    // smallest leaves at most.
+    float A = 0.f, E = 0.f;
+    if (!B.nodes.empty())
+        for (int k = 0; k < 3; ++k) {
+            A = std::max(A, std::max(std::fabs(B.nodes[0].lo[k]), std::fabs(B.nodes[0].hi[k])));
+            E = std::max(E, 0.5f * (B.nodes[0].hi[k] - B.nodes[0].lo[k]));
+        }
+    const float delta = 4e-6f * (A + E) + 1e-30f;
+    std::vector<nr::GpuNode> gf(gn);
+    for (auto& g : gf) {
+        g.a = make_float4(g.a.x - delta, g.a.y + delta, g.a.z - delta, g.a.w + delta);
+        g.b = make_float4(g.b.x - delta, g.b.y + delta, g.b.z - delta, g.b.w + delta);
+        g.c = make_float4(g.c.x - delta, g.c.y + delta, g.c.z - delta, g.c.w + delta);
+    }
 
     // emitters in loader order, weight = Triangle::area (twice the area)
     std::vector<float4> lt;
@@ -312,6 +337,7 @@ void upload_scene(nr_scene* s) {
     upload(s->tri_geo, geo, st);
     upload(s->tri_shade, shade, st);
     upload(s->nodes, gn, st);
+    upload(s->nodes_fast, gf, st);
     upload(s->mats, H.mats, st);
     upload(s->texels, texels, st);
     upload(s->tex_info, tinfo, st);
@@ -326,6 +352,8 @@ void upload_scene(nr_scene* s) {
 
     nr::DeviceScene& D = s->dev;
     D.nodes = s->nodes.as<nr::GpuNode>();
+    D.nodes_fast = s->nodes_fast.as<nr::GpuNode>();
+    D.fast_origin_bound = 2.0f * A + 4.0f * E;
     D.tri_geo = s->tri_geo.as<float4>();
     D.tri_shade = s->tri_shade.as<float4>();
     D.mats = s->mats.as<nr_material>();
@@ -558,6 +586,16 @@ struct RenderArgs {
     int64_t adj_rec_bytes;  // the adjoint's per-bounce hit and visibility records: at most this many bytes
                             // (0: none; the replay traces every bounce again from the Philox keys)
 };
+
+// The traversal mode a render can use: the widened-box walk (trav=1)
+// holds for ray origins inside the scene's origin bound, which every
+// surface point meets; a camera outside it gets the exact walk (trav=0,
+// the same hits).
+void check_camera(const nr_scene* s, RenderArgs& A) {
+    const float b = s->dev.fast_origin_bound;
+    for (int k = 0; k < 3; ++k)
+        if (!(std::fabs(A.cam.pos[k]) <= b)) A.pol.trav = 0;
+}
 
 // The scene as the kernels of one call see it: the pruning factor of the
 // call's traversals.
@@ -1096,6 +1134,7 @@ int nr_adjoint(nr_scene* s, const nr_camera* cam, const char* params, const floa
         with_oom_release(s, [&]() {
             NR_CUDA(cudaSetDevice(s->device));
             RenderArgs A = parse_args(cam, params);
+            check_camera(s, A);
             if (A.pol.excl) throw NrError(NR_ERR_INVALID, "the adjoint differentiates renderer=ptnee or pt");
             if (A.pol.envis) throw NrError(NR_ERR_INVALID, "the adjoint does not support envis");
             const int npix = A.pol.imgw * A.pol.imgh;
@@ -1270,6 +1309,7 @@ int nr_render(nr_scene* s, const nr_camera* cam, const char* params, float* hdr_
         with_oom_release(s, [&]() {
             NR_CUDA(cudaSetDevice(s->device));
             RenderArgs A = parse_args(cam, params);
+            check_camera(s, A);
             const int npix = A.pol.imgw * A.pol.imgh;
             cudaStream_t st = s->stream;
             if (s->film.bytes < (size_t)npix * sizeof(float4)) {
@@ -1319,6 +1359,7 @@ int nr_render_samples(nr_scene* s, const nr_camera* cam, const char* params, int
         with_oom_release(s, [&]() {
             NR_CUDA(cudaSetDevice(s->device));
             RenderArgs A = parse_args(cam, params);
+            check_camera(s, A);
             A.spp = spp;
             for (int32_t i = 0; i < npix; ++i)
                 if (pix_xy[2 * i] < 0 || pix_xy[2 * i] >= A.pol.imgw || pix_xy[2 * i + 1] < 0 || pix_xy[2 * i + 1] >= A.pol.imgh)

@@ -86,8 +86,16 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // Closest hit, persistent: warps take 32 queue entries at a time from a
 // shared cursor, one ray per lane to completion (closest_hit), then the slot
 // is bucketed by shading category (material type of the hit, or CAT_MISS).
-// FAST selects the box / triangle tests with exact fallback; both variants
-// return the same hits bit for bit. (Measured and dropped: a variant that
+// FAST (trav=1) walks the widened boxes with the one-FMA test alone and
+// tests triangles with the fast test and its exact fallback; !FAST (trav=0)
+// walks the reference's boxes with its exact arithmetic. The widened boxes
+// accept every box the exact test accepts, so trav=1 reaches every triangle
+// trav=0 reaches (the same hits but where a ray passes within about 1e-6 of
+// a box face and hits a triangle there that the exact test's rounding
+// excludes). Measured on the 1M-triangle frame: 757.5 Mpaths/s with the
+// margin-and-fallback box test on the reference's boxes, 866.4 with the
+// one-FMA test alone (not conservative), 831.3 with that test widened by its
+// error bound at run time. (Measured and dropped: a variant that
 // refilled idle lanes from the queue with separate node and leaf phases,
 // 28 % slower; a four-wide tree collapsed from this one, no faster.)
 // Minimum resident 128-thread blocks per SM requested from the register
@@ -147,7 +155,7 @@ __global__ void __launch_bounds__(128, NR_TRACE_MINB) k_trace(PathState P, Devic
             int slot = P.queue_in[idx];
             f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
             float t, b1, b2;
-            int tri = (NR_WW & 9) ? closest_hit_ww<FAST, (NR_WW & 1) != 0, NR_SMEM_STACK>(
+            int tri = (NR_WW & 9) ? closest_hit_ww<FAST ? 2 : 0, (NR_WW & 1) != 0, NR_SMEM_STACK>(
                                         S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
                                         COUNT ? &nt : nullptr, ring)
                             : closest_hit<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
@@ -203,7 +211,7 @@ __global__ void __launch_bounds__(128, NR_SHADOW_MINB) k_shadow(PathState P, Dev
             const bool env = o.w < 0.f;  // an environment sample: k_env_fold adds it
             const float tmax = env ? -o.w : o.w;
             const bool occluded =
-                (NR_WW & 6) ? any_hit_ww<FAST, (NR_WW & 2) != 0, NR_SMEM_STACK>(
+                (NR_WW & 6) ? any_hit_ww<FAST ? 2 : 0, (NR_WW & 2) != 0, NR_SMEM_STACK>(
                                   S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
                                   COUNT ? &nt : nullptr, ring)
                       : any_hit<FAST>(S, xyz(o), xyz(d), tmax, &P.counters[CNT_ERR], COUNT ? &nv : nullptr,
@@ -272,8 +280,8 @@ __device__ __forceinline__ void emit_shadow(const PathState& P, const DeviceScen
                                             const NrcCtx& C, int slot, int rec, f3 so, f3 d, float tmax, f3 c,
                                             bool env = false) {
     if (TAIL && tmax > 0.f) {
-        const bool occluded = pol.trav ? any_hit_ww<true, (NR_WW & 2) != 0>(S, so, d, tmax, &P.counters[CNT_ERR])
-                                       : any_hit_ww<false, (NR_WW & 2) != 0>(S, so, d, tmax, &P.counters[CNT_ERR]);
+        const bool occluded = pol.trav ? any_hit_ww<2, (NR_WW & 2) != 0>(S, so, d, tmax, &P.counters[CNT_ERR])
+                                       : any_hit_ww<0, (NR_WW & 2) != 0>(S, so, d, tmax, &P.counters[CNT_ERR]);
         if (occluded) return;
         tmax = 0.f;  // unoccluded: added below
     }
@@ -541,7 +549,7 @@ __global__ void __launch_bounds__(128, 4) k_tail(PathState P, DeviceScene S, Pol
     for (int b = 0; b < NR_TAIL_MAX_BOUNCES; ++b) {
         const f3 o = xyz(P.ray_o[slot]), d = xyz(P.ray_d[slot]);
         float t, b1, b2;
-        const int tri = closest_hit_ww<FAST>(S, o, d, t, b1, b2, &P.counters[CNT_ERR]);
+        const int tri = closest_hit_ww<FAST ? 2 : 0>(S, o, d, t, b1, b2, &P.counters[CNT_ERR]);
         P.hit[slot] = make_float4(t, b1, b2, __int_as_float(tri));
         if (!shade_one<NRC, -1, true>(P, S, pol, slot, C)) return;
     }

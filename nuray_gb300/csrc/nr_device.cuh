@@ -7,12 +7,6 @@
 
 #include "nr_types.h"
 
-// Build-time switch for measurements: 1 takes the one-FMA slab test's
-// answer without its error margin and exact fallback.
-#ifndef NR_BOX_PLAIN
-#define NR_BOX_PLAIN 0
-#endif
-
 namespace nr {
 
 // ------------------------------------------------------------------ vectors
@@ -164,15 +158,39 @@ __device__ __forceinline__ bool box_test_fast(const SlabRay& r, float lx, float 
     float z1 = __fmaf_rn(lz, r.rz, r.cz), z2 = __fmaf_rn(hz, r.rz, r.cz);
     float tin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fmaxf(fminf(z1, z2), -1e18f));
     float tout = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fminf(fmaxf(z1, z2), 1e18f));
-#if NR_BOX_PLAIN
-    t_entry = tin;
-    return tin <= tout && tout >= 0.0f;
-#endif
     float margin = 1e-6f * fmaxf(fabsf(tin), fabsf(tout)) + r.abs_err;
     if (tout < -margin) return false;
     if (tin + margin < tout && tout > margin) { t_entry = tin; return true; }
     if (tin > tout + margin) return false;
     return box_test(r, lx, hx, ly, hy, lz, hz, t_entry);
+}
+
+// The one-FMA test alone, for boxes widened on the host (DeviceScene::
+// nodes_fast): each bound is moved outward by more than the error of these
+// quotients and of the reference's own rounding for every ray origin within
+// DeviceScene::fast_origin_bound, so the test accepts every box the exact
+// test accepts for the unwidened box (and a sliver more around it) without
+// a margin or a fallback.
+__device__ __forceinline__ bool box_test_plain(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                               float& t_entry) {
+    float x1 = __fmaf_rn(lx, r.rx, r.cx), x2 = __fmaf_rn(hx, r.rx, r.cx);
+    float y1 = __fmaf_rn(ly, r.ry, r.cy), y2 = __fmaf_rn(hy, r.ry, r.cy);
+    float z1 = __fmaf_rn(lz, r.rz, r.cz), z2 = __fmaf_rn(hz, r.rz, r.cz);
+    float tin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fmaxf(fminf(z1, z2), -1e18f));
+    float tout = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fminf(fmaxf(z1, z2), 1e18f));
+    t_entry = tin;
+    return tin <= tout && tout >= 0.0f;
+}
+
+// Box test of traversal mode MODE: 0 the reference's exact arithmetic, 1 the
+// one-FMA test with its error margin and exact fallback (the same answers),
+// 2 box_test_plain on the widened boxes.
+template <int MODE>
+__device__ __forceinline__ bool box_test_mode(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                              float& t_entry) {
+    if (MODE == 0) return box_test(r, lx, hx, ly, hy, lz, hz, t_entry);
+    if (MODE == 1) return box_test_fast(r, lx, hx, ly, hy, lz, hz, t_entry);
+    return box_test_plain(r, lx, hx, ly, hy, lz, hz, t_entry);
 }
 
 // Triangle::intersection (src/scene/triangle.cpp:27-33) followed by the leaf
@@ -403,7 +421,7 @@ struct TravStack {
     }
 };
 
-template <bool FAST, bool SPEC = true, int K = 0>
+template <int MODE, bool SPEC = true, int K = 0>
 __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, float& best_t, float& best_b1,
                                               float& best_b2, uint32_t* err, uint32_t* nodes_visited = nullptr,
                                               uint32_t* tris_tested = nullptr, int2* ring = nullptr) {
@@ -430,13 +448,13 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
     while (ref != NR_TRAV_END) {
         while ((unsigned)ref < (unsigned)NR_TRAV_END) {
             if (--budget < 0) { atomicOr(err, 2u); ref = NR_TRAV_END; leaf = 0; break; }
-            const GpuNode& N = S.nodes[ref];
+            const GpuNode& N = (MODE == 2 ? S.nodes_fast : S.nodes)[ref];
             float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
             int4 k = __ldg(&N.d);
             ++nv;
             float t0, t1;
-            bool h0 = FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
-            bool h1 = FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
+            bool h0 = box_test_mode<MODE>(R, a.x, a.y, a.z, a.w, c.x, c.y, t0);
+            bool h1 = box_test_mode<MODE>(R, b.x, b.y, b.z, b.w, c.z, c.w, t1);
             const float lim = best_t * S.prune_k;
             h0 = h0 && t0 <= lim;
             h1 = h1 && t1 <= lim;
@@ -480,7 +498,7 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
                 // best_t as the limit rejects farther hits before the exact
                 // quotients (770.9 -> 772.8 Mpaths/s)
                 const float cap = fminf(lt, __uint_as_float(__float_as_uint(best_t) + 1u));
-                if (FAST ? tri_test_fast(o, d, g0, g1, g2, cap, t, u, v) : tri_test(o, d, g0, g1, g2, cap, t, u, v)) {
+                if (MODE ? tri_test_fast(o, d, g0, g1, g2, cap, t, u, v) : tri_test(o, d, g0, g1, g2, cap, t, u, v)) {
                     lt = t; li = ti;
                 }
             }
@@ -504,7 +522,7 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
 
 // Any hit with t <= tmax, traversed as closest_hit_ww (SPEC), or while-while
 // without postponing: a lane's inner-node loop ends at its first leaf.
-template <bool FAST, bool SPEC, int K = 0>
+template <int MODE, bool SPEC, int K = 0>
 __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, float tmax, uint32_t* err,
                                            uint32_t* nodes_visited = nullptr, uint32_t* tris_tested = nullptr,
                                            int* ring = nullptr) {
@@ -522,13 +540,13 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
     while (ref != NR_TRAV_END) {
         while ((unsigned)ref < (unsigned)NR_TRAV_END) {
             if (--budget < 0) { atomicOr(err, 2u); return false; }
-            const GpuNode& N = S.nodes[ref];
+            const GpuNode& N = (MODE == 2 ? S.nodes_fast : S.nodes)[ref];
             float4 a = __ldg(&N.a), b = __ldg(&N.b), c = __ldg(&N.c);
             int4 k = __ldg(&N.d);
             if (nodes_visited) ++*nodes_visited;
             float t0, t1;
-            bool h0 = (FAST ? box_test_fast(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) : box_test(R, a.x, a.y, a.z, a.w, c.x, c.y, t0)) && t0 <= lim;
-            bool h1 = (FAST ? box_test_fast(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) : box_test(R, b.x, b.y, b.z, b.w, c.z, c.w, t1)) && t1 <= lim;
+            bool h0 = box_test_mode<MODE>(R, a.x, a.y, a.z, a.w, c.x, c.y, t0) && t0 <= lim;
+            bool h1 = box_test_mode<MODE>(R, b.x, b.y, b.z, b.w, c.z, c.w, t1) && t1 <= lim;
             if (h0 && h1) {
                 int nr = k.x, fr = k.y;
                 // far child first: the near one holds the surface the shadow
@@ -564,7 +582,7 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
                 float4 g0 = __ldg(&S.tri_geo[3 * ti]), g1 = __ldg(&S.tri_geo[3 * ti + 1]), g2 = __ldg(&S.tri_geo[3 * ti + 2]);
                 if (tris_tested) ++*tris_tested;
                 float t, u, v;
-                if (FAST ? tri_test_fast(o, d, g0, g1, g2, limit, t, u, v) : tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
+                if (MODE ? tri_test_fast(o, d, g0, g1, g2, limit, t, u, v) : tri_test(o, d, g0, g1, g2, limit, t, u, v)) return true;
             }
             leaf = ref;
             if (ref < 0) ref = stack.empty() ? NR_TRAV_END : stack.pop();

@@ -67,6 +67,8 @@ struct DeviceScene {
     int32_t max_depth;        // deepest leaf (root = 0)
     int32_t num_nodes;        // internal nodes
     float prune_k;            // subtrees entered beyond prune_k x the best hit are skipped (infinity: none)
+    const GpuNode* nodes_fast;  // the same nodes with every box widened for box_test_plain (traversal mode 2)
+    float fast_origin_bound;    // mode 2 is conservative for ray origins with every |coordinate| <= this
 };
 
 // Render policy decoded from the parameter string.

@@ -125,11 +125,43 @@ __device__ void load_w(unsigned char* sm, int off, const __nv_bfloat16* __restri
 // `wb` and the biases of `params`; out [rows][3] FP32; acts (may be null):
 // the hidden layers' post-ReLU BF16 activations [4][R.ld][64] for the
 // backward pass. err bit 8 on a tensor-core wait that timed out.
-__global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __restrict__ wb,
-                                                        const float* __restrict__ params,
-                                                        const __nv_bfloat16* __restrict__ x, NrcRows R,
-                                                        float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
-                                                        uint32_t* err, uint32_t first_wait) {
+//
+// NWG warpgroups per CTA, each an independent tile pipeline over the one
+// copy of the weights in shared memory: its own 128-row A buffer, mbarrier
+// and 64 tensor-memory columns, synchronised by its own named barrier. One
+// tile's five layers are a dependent chain (MMA, commit, wait, tensor-memory
+// read, epilogue), so tiles in flight are what hides that latency: with
+// NWG = 3 two CTAs fit an SM (98 KB of shared memory each, 256 tensor-memory
+// columns each), six tiles in flight per SM against three with one
+// warpgroup per CTA.
+namespace {
+constexpr int FW_A_BYTES = (TM / 8) * KC_IN * 128;          // 128 x 80 BF16, canonical layout
+constexpr int FW_BIAS = SM_A;                               // biases right after the weights
+constexpr int FW_ABUF = ((FW_BIAS + (4 * H + 16) * 4) + 127) / 128 * 128;
+__host__ __device__ constexpr int fw_smem(int nwg) { return FW_ABUF + nwg * FW_A_BYTES + 16 * nwg; }
+__host__ __device__ constexpr uint32_t fw_tmem_cols(int nwg) { return nwg == 1 ? 64u : (nwg == 2 ? 128u : 256u); }
+
+// Named barrier `id` over the 128 threads of one warpgroup.
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;\n" ::"r"(id) : "memory"); }
+// The same with an OR of v over the warpgroup.
+__device__ __forceinline__ bool wg_sync_or(int id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n barrier.cta.red.or.pred p, %2, 128, q;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+}  // namespace
+
+template <int NWG>
+__global__ void __launch_bounds__(128 * NWG) k_nrc_forward_tc(const __nv_bfloat16* __restrict__ wb,
+                                                              const float* __restrict__ params,
+                                                              const __nv_bfloat16* __restrict__ x, NrcRows R,
+                                                              float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
+                                                              uint32_t* err, uint32_t first_wait) {
     int m0, M;
     if (!R.count) {
         m0 = 0;
@@ -141,16 +173,17 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
         M = max(0, min(chunk, total - m0));
     }
     const int tiles = (M + TM - 1) / TM;
-    if ((int)blockIdx.x >= tiles) return;  // the whole CTA: no tensor memory taken
+    if ((int)blockIdx.x * NWG >= tiles) return;  // no warpgroup of this CTA has a tile: no tensor memory taken
     x += (size_t)m0 * IN;
     out += (size_t)m0 * 3;
     const size_t LS = (size_t)R.ld * H;  // one layer of acts
 
     extern __shared__ __align__(1024) unsigned char sm[];
-    float* sbias = reinterpret_cast<float*>(sm + SM_BIAS);
+    float* sbias = reinterpret_cast<float*>(sm + FW_BIAS);
     __shared__ uint32_t s_taddr;
-    __shared__ int s_abort;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    __shared__ int s_abort[NWG];
+    const int tid = threadIdx.x, warp = tid >> 5, wg = tid >> 7, wtid = tid & 127;
+    const int bar_id = 1 + wg;  // named barrier of this warpgroup (0 is __syncthreads)
 
     load_w(sm, SM_W0, wb + NRC_OFF_W0, H, H, IN);
     load_w(sm, SM_W1, wb + NRC_OFF_W1, H, H, H);
@@ -162,33 +195,35 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
         sbias[i] = i < 4 * H ? params[offs[i / H] + i % H]
                              : (i - 4 * H < NRC_OUT_PAD ? params[NRC_OFF_B4 + i - 4 * H] : 0.f);
     }
-    const uint32_t bar = smem_u32(sm + SM_BAR);
-    if (tid == 0) {
-        s_abort = 0;
+    unsigned char* abuf = sm + FW_ABUF + wg * FW_A_BYTES;
+    const uint32_t bar = smem_u32(sm + FW_ABUF + NWG * FW_A_BYTES + 16 * wg);
+    if (wtid == 0) {
+        s_abort[wg] = 0;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_taddr)),
-                     "r"(TMEM_COLS)
+                     "r"(fw_tmem_cols(NWG))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = s_taddr;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    // this warpgroup's 64 columns; a warp reads the tensor-memory lanes of its quarter
+    const uint32_t tmem = s_taddr + 64u * (uint32_t)wg;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     uint32_t phase = 0;
 
-    const uint32_t a_addr = smem_u32(sm + SM_A);
+    const uint32_t a_addr = smem_u32(abuf);
     const uint32_t w_addr[5] = {smem_u32(sm + SM_W0), smem_u32(sm + SM_W1), smem_u32(sm + SM_W2), smem_u32(sm + SM_W3),
                                 smem_u32(sm + SM_W4)};
 
-    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (int tile = blockIdx.x * NWG + wg; tile < tiles; tile += gridDim.x * NWG) {
         {  // input rows -> A (K = 80)
-            const int r = tid, row = tile * TM + r;
-            unsigned char* dst = sm + SM_A + (r / 8) * (KC_IN * 128) + (r % 8) * 16;
+            const int r = wtid, row = tile * TM + r;
+            unsigned char* dst = abuf + (r / 8) * (KC_IN * 128) + (r % 8) * 16;
 #pragma unroll
             for (int c = 0; c < KC_IN; ++c) {
                 uint4 v = make_uint4(0u, 0u, 0u, 0u);
@@ -202,8 +237,8 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
             const uint32_t n = layer == 4 ? 16u : (uint32_t)H;
             fence_async_smem();
             fence_before();
-            __syncthreads();
-            if (tid == 0) {
+            wg_sync(bar_id);
+            if (wtid == 0) {
                 fence_after();
 #pragma unroll 1
                 for (int ks = 0; ks < k / 16; ++ks) {
@@ -214,9 +249,9 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
                 commit(bar);
             }
             const bool ok = wait_phase(bar, phase, first_wait);
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    s_abort = 1;
+            if (wg_sync_or(bar_id, !ok)) {
+                if (wtid == 0) {
+                    s_abort[wg] = 1;
                     // the MMAs may still write the tensor memory freed below:
                     // one more bounded wait for their commit; if that runs
                     // out too, bit 32 tells the host to stop using these kernels
@@ -227,9 +262,9 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
             }
             phase ^= 1u;
             fence_after();
-            const int r = tid, row = tile * TM + r;
+            const int r = wtid, row = tile * TM + r;
             if (layer < 4) {
-                unsigned char* dst = sm + SM_A + (r / 8) * (KC_H * 128) + (r % 8) * 16;
+                unsigned char* dst = abuf + (r / 8) * (KC_H * 128) + (r % 8) * 16;
                 const float* b = sbias + layer * H;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -258,14 +293,15 @@ __global__ void __launch_bounds__(128) k_nrc_forward_tc(const __nv_bfloat16* __r
                 }
             }
         }
-        __syncthreads();
-        if (s_abort) break;
+        wg_sync(bar_id);
+        if (s_abort[wg]) break;
     }
     fence_before();
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(s_taddr), "r"(fw_tmem_cols(NWG))
+                     : "memory");
     }
 }
 
@@ -453,7 +489,13 @@ __global__ void __launch_bounds__(128) k_nrc_backward_data_tc(const __nv_bfloat1
     }
 }
 
-size_t nrc_forward_tc_smem() { return (size_t)SM_TOTAL; }
+// Warpgroups per CTA of the forward kernel (NR_NRC_FW_WG: 1, 2 or 3).
+#ifndef NR_NRC_FW_WG
+#define NR_NRC_FW_WG 3
+#endif
+constexpr int kFwWg = NR_NRC_FW_WG;
+static_assert(kFwWg >= 1 && kFwWg <= 3, "1 to 3 warpgroups per forward CTA");
+size_t nrc_forward_tc_smem() { return (size_t)fw_smem(kFwWg); }
 
 namespace {
 std::atomic<bool> g_tc_disabled{false};
@@ -462,7 +504,7 @@ void nrc_tc_disable() { g_tc_disabled.store(true); }
 bool nrc_tc_enabled() { return !g_tc_disabled.load(); }
 
 void nrc_tc_setup() {
-    cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc_forward_tc_smem());
+    cudaFuncSetAttribute(k_nrc_forward_tc<kFwWg>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc_forward_tc_smem());
     cudaFuncSetAttribute(k_nrc_backward_data_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, BK_TOTAL);
 }
 
@@ -471,10 +513,13 @@ void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const _
                            uint32_t first_wait) {
     const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
     if (M <= 0) return;
-    int blocks = (M + TM - 1) / TM;
-    const int cap = num_sms * 3;  // three resident CTAs per SM by shared memory (64 tensor-memory columns each)
+    const int tiles = (M + TM - 1) / TM;
+    int blocks = (tiles + kFwWg - 1) / kFwWg;
+    // resident CTAs per SM by shared memory: 3 with one warpgroup (58 KB), 2 with two or three
+    const int cap = num_sms * (kFwWg == 1 ? 3 : 2);
     if (blocks > cap) blocks = cap;
-    k_nrc_forward_tc<<<blocks, 128, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, acts, err, first_wait);
+    k_nrc_forward_tc<kFwWg><<<blocks, 128 * kFwWg, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, acts, err,
+                                                                              first_wait);
 }
 
 size_t nrc_wt_image_bytes() { return (size_t)BK_A; }

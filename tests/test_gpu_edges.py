@@ -195,3 +195,16 @@ def test_endless_paths_stop_with_an_error(gpu_lib, tail):
         S.render(p + f" prr=1 maxdepth=0 tail={tail}")
     img = S.render(p + f" tail={tail}")  # default prr: paths end, no light: black
     assert np.all(img == 0)
+
+
+def test_camera_outside_the_widened_box_bound_takes_the_exact_walk(gpu_lib):
+    """trav=1 walks boxes widened for ray origins inside the scene's origin
+    bound (twice the largest coordinate plus four half extents); a camera
+    outside it makes the render take the exact walk (trav=0), so both give
+    the same image bit for bit."""
+    S = gpu_scene(cornell_scene())
+    far = CORNELL.replace("campos=0,120,200", "campos=0,120,40000").replace("camfov=64", "camfov=2")
+    a = S.render(far)
+    b = S.render(far + " trav=0")
+    np.testing.assert_array_equal(a, b)
+    assert a.mean() > 0

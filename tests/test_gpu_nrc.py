@@ -193,15 +193,16 @@ def test_nrc_render_close_to_reference(gpu_lib):
 def test_tensor_core_forward_equals_mma_sync(gpu_lib):
     """The two inference kernels on the same BF16 weights and inputs: FP32
     accumulation in a different order, hidden activations rounded to BF16 by
-    both, so the outputs agree closely; 1, 127, 128, 129 and 5000 rows cover
-    partial and several 128-row tiles."""
+    both, so the outputs agree closely; 1, 127, 128, 129, 257, 385, 5000 and
+    100000 rows cover partial tiles, CTAs whose three warpgroups hold one,
+    two or three tiles, and many tiles per warpgroup."""
     from nuray_gb300.nrc import Cache
     a, b = Cache("seed=4 tc=1"), Cache("seed=4 tc=0")
     rng = np.random.default_rng(2)
     p = a.get_params() + rng.normal(scale=0.05, size=a.get_params().size).astype(np.float32)
     a.set_params(p)
     b.set_params(p)
-    for n in (1, 127, 128, 129, 5000):
+    for n in (1, 127, 128, 129, 257, 385, 5000, 100000):
         x = rand_inputs(n, n)
         ya, yb = a.infer(x), b.infer(x)
         # the forward tolerance of this file: a hidden activation near a BF16
