@@ -206,8 +206,14 @@ def test_tensor_core_forward_equals_mma_sync(gpu_lib):
         x = rand_inputs(n, n)
         ya, yb = a.infer(x), b.infer(x)
         # the forward tolerance of this file: a hidden activation near a BF16
-        # rounding boundary can round the other way under the other order
-        np.testing.assert_allclose(ya, yb, rtol=1e-2, atol=2e-3)
+        # rounding boundary can round the other way under the other order,
+        # which moves an output by about one BF16 step of the activation
+        # times a weight; over 100k rows a few such flips reach past it, so
+        # the tolerance holds for all but 1e-4 of the outputs, and no output
+        # moves by more than 1e-2
+        close = np.isclose(ya, yb, rtol=1e-2, atol=2e-3)
+        assert close.mean() >= 1 - 1e-4, n
+        assert np.abs(ya - yb).max() <= 1e-2, n
         assert np.mean(np.abs(ya - yb) <= 1e-5 + 1e-4 * np.abs(yb)) > 0.99
 
 
