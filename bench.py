@@ -60,10 +60,11 @@ BYTES_TRI = 36
 # instructions (smsp__inst_executed.sum over the launch's rays), which give
 # the issue roofline: instructions / (SMs x 4 schedulers x clock x time).
 NCU_CAPTURE = {
-    "what": "one ncu capture, 480x270 x 32 spp frame of the same scene, bounce-0 launches",
-    "k_trace": {"dram_bytes_per_ray": 62.2, "l2_hit_rate": 0.675, "l1_hit_rate": 0.796,
-                "warp_inst_per_ray": 185.7},
-    "k_shadow": {"warp_inst_per_ray": None},
+    "what": "ncu captures of a 480x270 x 32 spp frame of the same scene: DRAM bytes and hit rates of the bounce-0 "
+            "k_trace launch; warp instructions of all of the frame's k_trace / k_shadow launches over its rays",
+    "k_trace": {"dram_bytes_per_ray": 61.6, "l2_hit_rate": 0.637, "l1_hit_rate": 0.832,
+                "warp_inst_per_ray": 264.9},
+    "k_shadow": {"warp_inst_per_ray": 305.6},
 }
 SM_COUNT = 152
 
