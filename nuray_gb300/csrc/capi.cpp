@@ -580,6 +580,7 @@ struct RenderArgs {
     float nrc_rough;  // roughness from which a GGX vertex is diffuse
     int nrc_direct;   // 1: light sample at the query vertex, cache for the rest
     int nrc_train_depth;  // > 0: training paths end in the cache from this depth on
+    int nrc_first;        // 1: paths may end at their first diffuse vertex itself
     bool nrc_pre;         // renderer=nrc: one all-training pass before the samples (RendererNRC::render)
     bool adj_mega;        // adjoint replay as one thread per path (adj=mega) instead of the wavefront
     bool prune;           // 0: every node whose box a ray enters is visited, as the reference does
@@ -674,7 +675,8 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.nrc_train = c.get_int("nrc_train", 16384);
     a.nrc_steps = c.get_int("nrc_steps", 2);
     a.nrc_query = c.get_int("nrc_query", 1);
-    a.nrc_mindepth = nrc_mode ? c.get_int("path_lim", 2) : c.get_int("nrc_mindepth", 1);
+    a.nrc_first = nrc_mode ? 0 : (c.get_int("nrc_first", 0) != 0 ? 1 : 0);
+    a.nrc_mindepth = nrc_mode ? c.get_int("path_lim", 2) : c.get_int("nrc_mindepth", a.nrc_first ? 0 : 1);
     // GGX vertices from this roughness on count as diffuse for ending paths
     // in the cache. Time to relMSE 1e-3 at 960x540, 64 spp per frame: 2.78 s
     // at 0.2, 2.72 at 0.1, 2.69 at 0.05 and at 0 (plain PT 2.89).
@@ -756,6 +758,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         X.rough = A.nrc_rough;
         X.direct = A.nrc_direct;
         X.train_depth = A.nrc_train_depth;
+        X.first = A.nrc_first;
         for (int k = 0; k < 3; ++k) {
             float ext = s->dev.root_hi[k] - s->dev.root_lo[k];
             X.lo[k] = s->dev.root_lo[k];

@@ -365,7 +365,8 @@ __device__ __forceinline__ bool shade_one(const PathState& P, const DeviceScene&
         // renderer=nrc asks at any vertex: depth >= path_lim, or
         // path_lim_train on training paths (renderernrc.cpp:130).
         const bool end_here = train ? (C.train_depth > 0 && depth >= C.train_depth) : depth >= C.min_depth;
-        if ((flags || pol.excl) && C.query && end_here) {
+        const bool diffuse_here = C.first && nrc_diffuse(M, C.rough);
+        if ((flags || diffuse_here || pol.excl) && C.query && end_here) {
             int q = warp_append(true, &C.counters[0]);
             C.q_slot[q] = slot;
             C.q_thr[q] = make_float4(T.x, T.y, T.z, 0.f);

@@ -131,6 +131,7 @@ struct NrcCtx {
     int32_t train_depth;    // > 0: training paths end in the cache from this vertex depth on
     int32_t direct;         // 1: the cache holds radiance after the vertex's own light sample
                             // (queries still sample a light); 0: all outgoing radiance
+    int32_t first;          // 1: a path may end at its first diffuse vertex itself, not only after it
     float lo[3], inv_ext[3];  // scene box for the position encoding
 };
 
