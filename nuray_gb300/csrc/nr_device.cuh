@@ -391,17 +391,6 @@ __device__ __forceinline__ int closest_hit(const DeviceScene& S, f3 o, f3 d, flo
 // Refs: inner nodes >= 0, leaves < 0; NR_TRAV_END (no node) ends the walk.
 #define NR_TRAV_END 0x7fffffff
 
-// Build-time switch for measurements: prefetch into L1 the node (or the
-// leaf's first triangle) of a subtree as it is pushed, for the any-hit
-// walk (bit 1) and the closest-hit walk (bit 2).
-#ifndef NR_PREFETCH
-#define NR_PREFETCH 0
-#endif
-__device__ __forceinline__ void prefetch_ref(const DeviceScene& S, const GpuNode* nodes, int ref) {
-    const void* p = ref >= 0 ? (const void*)&nodes[ref] : (const void*)&S.tri_geo[3 * leaf_first(ref)];
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
 // Traversal stacks. The default keeps every entry in per-thread local
 // memory (L1-resident). With K > 0 the top K entries of each thread live in
 // a shared-memory ring (entry i at ring[(i % K) * blockDim.x]: threads of a
@@ -475,7 +464,6 @@ __device__ __forceinline__ int closest_hit_ww(const DeviceScene& S, f3 o, f3 d, 
                 if (t1 < t0) { nr = k.y; fr = k.x; ft = t0; }
                 if (stack.full()) { atomicOr(err, 1u); ref = NR_TRAV_END; leaf = 0; break; }
                 stack.push(make_int2(fr, __float_as_int(ft)));
-                if (NR_PREFETCH & 2) prefetch_ref(S, MODE == 2 ? S.nodes_fast : S.nodes, fr);
                 ref = nr;
             } else if (h0) {
                 ref = k.x;
@@ -567,7 +555,6 @@ __device__ __forceinline__ bool any_hit_ww(const DeviceScene& S, f3 o, f3 d, flo
                 if (t1 > t0) { nr = k.y; fr = k.x; }
                 if (stack.full()) { atomicOr(err, 1u); return false; }
                 stack.push(fr);
-                if (NR_PREFETCH & 1) prefetch_ref(S, MODE == 2 ? S.nodes_fast : S.nodes, fr);
                 ref = nr;
             } else if (h0) {
                 ref = k.x;
