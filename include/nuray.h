@@ -374,7 +374,9 @@ int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, fl
  * query vertex still takes its light sample (shadow ray) and the cache
  * stands in only for the radiance after it; nrc_direct=0 makes the cache
  * stand in for all of it. A cache trained one way must be queried the same
- * way.
+ * way. nrc_first=1 lets a path end at its first diffuse vertex itself
+ * (nrc_mindepth then defaults to 0): a cheaper frame whose error stops at
+ * the cache's own bias.
  * NULL detaches. The cache must not be used through nr_nrc_* while a render
  * of the scene runs. */
 int nr_scene_attach_nrc(nr_scene* scene, nr_nrc* nrc);

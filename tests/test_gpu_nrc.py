@@ -190,6 +190,27 @@ def test_nrc_render_close_to_reference(gpu_lib):
     assert rel(img) < rel(plain)
 
 
+def test_nrc_first_ends_paths_at_the_first_diffuse_vertex(gpu_lib):
+    """nrc_first=1: query paths end at the camera's diffuse hit itself, so
+    the frame traces far fewer extension rays; the trained cache keeps the
+    image near the converged one (biased by the network's own error)."""
+    from nuray_gb300.nrc import Cache
+    S = cornell()
+    ref = S.render(PARAMS.replace("spp=16", "spp=2048") + " seed=7")
+    c = Cache("seed=0 lr=3e-3")
+    c.attach(S)
+    for k in range(30):
+        S.render(PARAMS + f" nrc=1 nrc_query=0 nrc_train=3072 sample0={16 * k}")
+    S.render(PARAMS + " nrc=1 nrc_train=3072 sample0=1000")
+    rays_default = S.stats()["rays"]
+    img = S.render(PARAMS + " nrc=1 nrc_train=3072 nrc_first=1 sample0=1000")
+    rays_first = S.stats()["rays"]
+    print(f"extension rays: default {rays_default}, nrc_first {rays_first}; mean ratio {img.mean() / ref.mean():.3f}")
+    assert np.all(np.isfinite(img)) and img.min() >= 0
+    assert rays_first < 0.7 * rays_default
+    assert abs(img.mean() / ref.mean() - 1) < 0.15
+
+
 def test_tensor_core_forward_equals_mma_sync(gpu_lib):
     """The two inference kernels on the same BF16 weights and inputs: FP32
     accumulation in a different order, hidden activations rounded to BF16 by
