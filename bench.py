@@ -62,9 +62,9 @@ BYTES_TRI = 36
 NCU_CAPTURE = {
     "what": "ncu captures of a 480x270 x 32 spp frame of the same scene: DRAM bytes and hit rates of the bounce-0 "
             "k_trace launch; warp instructions of all of the frame's k_trace / k_shadow launches over its rays",
-    "k_trace": {"dram_bytes_per_ray": 61.6, "l2_hit_rate": 0.637, "l1_hit_rate": 0.832,
-                "warp_inst_per_ray": 264.9},
-    "k_shadow": {"warp_inst_per_ray": 305.6},
+    "k_trace": {"dram_bytes_per_ray": 61.6, "l2_hit_rate": 0.631, "l1_hit_rate": 0.836,
+                "warp_inst_per_ray": 243.9},
+    "k_shadow": {"warp_inst_per_ray": 299.2},
 }
 SM_COUNT = 152
 

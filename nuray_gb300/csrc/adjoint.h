@@ -20,13 +20,16 @@ struct AdjArgs {
 // -1 for none; roughness terms and d fac / d alpha in pa), and per shadow ray
 // the light sample's gradient terms (sg0: albedo, roughness; sg1: emission,
 // w = material | light material << 16).
+// The adjoint's per-slot state in pairs that are read together, one
+// 32-byte sector per slot and pair (SlotField): (L, delta), (pk, pa), and
+// per shadow-queue entry (sg0, sg1).
 struct AdjWave {
-    float4* L;
-    float4* delta;
-    float4* pk;
-    float4* pa;
-    float4* sg0;
-    float4* sg1;
+    SlotField<float4> L;
+    SlotField<float4> delta;
+    SlotField<float4> pk;
+    SlotField<float4> pa;
+    SlotField<float4> sg0;
+    SlotField<float4> sg1;
 };
 // W: the wave (its layout as rendered); the radiance buffer and dldi are
 // indexed by scanline pixel, Lbuf as (pixel * spp + sample) * 3.

@@ -253,6 +253,25 @@ void upload_scene(nr_scene* s) {
         g.d = make_int4(ref_of(N.left), ref_of(N.right), N.depth, 0);
     }
     s->num_gpu_nodes = ng;
+    // The traversal loops rely on this shape rather than counting steps:
+    // every inner node is the child of at most one inner node, which has a
+    // smaller index, and every leaf's triangles lie within the scene. A walk
+    // then visits each node at most once and ends, and its stack holds at most
+    // max_depth entries (checked against NR_STACK_LIMIT before the upload).
+    {
+        std::vector<uint8_t> referenced(ng, 0);
+        auto check_child = [&](int parent, int r) {
+            if (r >= 0) {
+                if (r <= parent || r >= ng || referenced[r]++) throw NrError(NR_ERR_INVALID, "BVH is not a tree");
+            } else if (nr::leaf_first(r) < 0 || nr::leaf_first(r) + nr::leaf_count(r) > n) {
+                throw NrError(NR_ERR_INVALID, "BVH leaf outside the triangle array");
+            }
+        };
+        for (int i = 0; i < ng; ++i) {
+            check_child(i, gn[i].d.x);
+            check_child(i, gn[i].d.y);
+        }
+    }
 
     // The same nodes with every child box widened by delta for the one-FMA
     // box test without margin (traversal mode 2). For a ray origin o with
@@ -472,12 +491,14 @@ void ensure_paths(nr_scene* s, int cap, int sh_mult = 1) {
     char* p = s->path_mem.as<char>();
     auto take = [&](size_t n) { char* r = p; p += (n + 255) & ~size_t(255); return r; };
     nr::PathState& P = s->ps;
-    P.ray_o = (float4*)take(C * f4);
-    P.ray_d = (float4*)take(C * f4);
+    float4* od = (float4*)take(2 * C * f4);  // (ray_o, ray_d) per slot
+    P.ray_o.p = od;
+    P.ray_d.p = od + 1;
+    float4* tm = (float4*)take(2 * C * f4);  // (thr, meta) per slot
+    P.thr.p = tm;
+    P.meta.p = (uint4*)(tm + 1);
     P.hit = (float4*)take(C * f4);
-    P.thr = (float4*)take(C * f4);
     P.rad = (float4*)take(C * f4);
-    P.meta = (uint4*)take(C * 16);
     P.queue_in = (int32_t*)take(C * 4);
     P.queue_out = (int32_t*)take(C * 4);
     P.sorted = (int32_t*)take(C * 4 * nr::NUM_CAT);
@@ -941,12 +962,12 @@ uint64_t adjoint_waves(nr_scene* s, const RenderArgs& A, int npix, const float* 
     char* p = s->adj_wave.as<char>();
     auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
     nr::AdjWave J;
-    J.L = (float4*)take(C * 16);
-    J.delta = (float4*)take(C * 16);
-    J.pk = (float4*)take(C * 16);
-    J.pa = (float4*)take(C * 16);
-    J.sg0 = (float4*)take(CS * 16);
-    J.sg1 = (float4*)take(CS * 16);
+    J.L.p = (float4*)take(2 * C * 16);
+    J.delta.p = J.L.p + 1;
+    J.pk.p = (float4*)take(2 * C * 16);
+    J.pa.p = J.pk.p + 1;
+    J.sg0.p = (float4*)take(2 * CS * 16);
+    J.sg1.p = J.sg0.p + 1;
     float4* rec_hit = (float4*)take(C * 16 * (size_t)depth_rec);
     uint8_t* rec_vis = (uint8_t*)take(C * (size_t)depth_rec);
     const float film_h = nr::film_height(A.cam);

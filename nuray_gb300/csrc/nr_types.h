@@ -90,14 +90,26 @@ struct Policy {
                       // its contribution is zero (the adjoint's first pass); radiance unchanged
 };
 
+// One 16-byte field of every slot, stored beside another field that is read
+// and written with it, so that a slot's pair fills one 32-byte sector: once
+// the category sort has scattered the slots, each separate 16-byte field
+// cost a whole sector. Pairs: (ray_o, ray_d) and (thr, meta). Measured
+// against separate arrays: 1M-triangle frame 901.5 / 898.1 Mpaths/s, with
+// textures, sky and dielectrics 698.0 / 693.8, adjoint 735.2 / 720.2.
+template <class T>
+struct SlotField {
+    T* p;
+    __host__ __device__ T& operator[](size_t i) const { return p[2 * i]; }
+};
+
 // Wavefront path state, structure of arrays, one slot per in-flight path.
 struct PathState {
-    float4* ray_o;   // (origin, unused)
-    float4* ray_d;   // (direction, unused)
+    SlotField<float4> ray_o;  // (origin, unused)
+    SlotField<float4> ray_d;  // (direction, unused), beside ray_o
     float4* hit;     // (t, b1, b2, flattened triangle bits or -1)
-    float4* thr;     // (throughput, light_fac)
+    SlotField<float4> thr;    // (throughput, light_fac)
     float4* rad;     // (radiance, unused)
-    uint4* meta;     // (pixel, sample, draws taken, vertex depth)
+    SlotField<uint4> meta;    // (pixel, sample, draws taken, vertex depth), beside thr
     // queues of slot indices
     int32_t* queue_in;
     int32_t* queue_out;
