@@ -110,8 +110,12 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // frame: if-if 585.5 Mpaths/s; postponed leaves in both 591.9 (k_trace
 // -14 %, k_shadow slower: its first leaf often holds the occluder); in
 // closest hit only 636.6; with any hit while-while without postponing 645.4;
-// closest hit without postponing too 606.6. With this shape the caps stay
+// closest hit without postponing too 606.6. With this shape the caps were
 // best at 10 / 10 (trace 8: 621.8, 12: 629.6; shadow 8: 639.9, 12: 603.1).
+// Once the closest-hit walk lost its step budget (one register less) and
+// took the folded box test, 12 blocks (40 registers, 28 bytes of spills)
+// overtook 10 for it: 912.2 against 901.4 Mpaths/s, 9 blocks 879.9; the
+// shadow kernel stays at 10 (8: 906.8, 12: 909.7, 10: 912.1).
 // Also measured and dropped for the shadow rays: dynamic fetch of new rays
 // into idle lanes (Aila and Laine 2009) at 4, 8 or 16 idle lanes, 571;
 // the shadow queue sorted by light (counting sort, 257 buckets) before the
@@ -121,7 +125,7 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // cell of a 4x4x4 grid holding the ray's end point (counting sort in shared
 // memory): 756.1 and 743.3 against 772.1.
 #ifndef NR_TRACE_MINB
-#define NR_TRACE_MINB 10
+#define NR_TRACE_MINB 12
 #endif
 #ifndef NR_SHADOW_MINB
 #define NR_SHADOW_MINB 10
