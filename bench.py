@@ -62,8 +62,8 @@ BYTES_TRI = 36
 NCU_CAPTURE = {
     "what": "ncu captures of a 480x270 x 32 spp frame of the same scene: DRAM bytes and hit rates of the bounce-0 "
             "k_trace launch; warp instructions of all of the frame's k_trace / k_shadow launches over its rays",
-    "k_trace": {"dram_bytes_per_ray": 61.6, "l2_hit_rate": 0.631, "l1_hit_rate": 0.836,
-                "warp_inst_per_ray": 243.9},
+    "k_trace": {"dram_bytes_per_ray": 63.1, "l2_hit_rate": 0.661, "l1_hit_rate": 0.823,
+                "warp_inst_per_ray": 248.8},
     "k_shadow": {"warp_inst_per_ray": 299.2},
 }
 SM_COUNT = 152
