@@ -165,6 +165,7 @@ struct nr_scene {
     int nrc_cap = 0, nrc_tcap = 0;
     nr::NrcCtx nrc_ctx{};
     float* nrc_pred = nullptr;
+    __nv_bfloat16* nrc_qx = nullptr;  // expanded query rows, for a cache on the mma.sync kernels only
     float nrc_last_loss = 0.f;
     double bvh_wall_ms = 0.0, bvh_device_ms = 0.0;  // last BVH build
     Budget budget;
@@ -458,6 +459,7 @@ void release_work_buffers(nr_scene* s) {
     s->film_pixels = 0;
     s->film_samples = 0;
     s->nrc_cap = s->nrc_tcap = 0;
+    s->nrc_qx = nullptr;
 }
 
 // Runs f, a call's work on scene s; an allocation failure inside frees the
@@ -750,16 +752,20 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
         if (!s->nrc) throw NrError(NR_ERR_INVALID, "nrc=1 needs a cache attached with nr_scene_attach_nrc");
         const int depth_cap = A.pol.maxdepth > 0 ? A.pol.maxdepth : 16;
         const int tcap = A.nrc_train * depth_cap;
-        if (cap > s->nrc_cap || tcap > s->nrc_tcap) {
+        // the tensor-core forward reads compact query records; the mma.sync
+        // one needs them expanded into rows of 80 first
+        const bool need_qx = !s->nrc->use_tc();
+        if (cap > s->nrc_cap || tcap > s->nrc_tcap || (need_qx && !s->nrc_qx)) {
             auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
             size_t C = (size_t)cap, T = (size_t)tcap;
             s->nrc_cap = s->nrc_tcap = 0;  // set again once the records are in place
-            s->nrc_mem.alloc(al(C * NRC_IN * 2) + al(C * 4) + al(C * 16) + al(T * NRC_IN * 2) + al(T * 4) + al(T * 16) * 2 +
-                             256 + al(C * 12));
+            s->nrc_qx = nullptr;
+            s->nrc_mem.alloc(al(C * 32) + al(C * 4) + al(C * 16) + al(T * NRC_IN * 2) + al(T * 4) + al(T * 16) * 2 +
+                             256 + al(C * 12) + (need_qx ? al(C * NRC_IN * 2) : 0));
             char* p = s->nrc_mem.as<char>();
             auto take = [&](size_t b) { char* r = p; p += al(b); return r; };
             nr::NrcCtx& X = s->nrc_ctx;
-            X.q_x = take(C * NRC_IN * 2);
+            X.q_rec = (uint4*)take(C * 32);
             X.q_slot = (int32_t*)take(C * 4);
             X.q_thr = (float4*)take(C * 16);
             X.t_x = take(T * NRC_IN * 2);
@@ -768,6 +774,7 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             X.t_before = (float4*)take(T * 16);
             X.counters = (uint32_t*)take(16);
             s->nrc_pred = (float*)take(C * 12);
+            if (need_qx) s->nrc_qx = (__nv_bfloat16*)take(C * NRC_IN * 2);
             s->nrc_cap = cap;
             s->nrc_tcap = tcap;
         }
@@ -869,13 +876,16 @@ void run_waves(nr_scene* s, const RenderArgs& A, int npix, const int32_t* dev_pi
             // launch reads them there, so the host never waits here.
             nr_nrc* c = s->nrc;
             const nr::NrcCtx& X = s->nrc_ctx;
-            if (c->use_tc())
-                nr::nrc_launch_forward_tc(c->dev.wb_inf, c->dev.pinf, (const __nv_bfloat16*)X.q_x,
-                                          nr::nrc_rows_counted(&X.counters[0], cap, 0, 1), s->nrc_pred, c->num_sms,
-                                          s->ps.counters + nr::CNT_ERR, st, nullptr, c->tc_first_wait);
-            else
-                nr::nrc_launch_forward_inf(c->dev, (const __nv_bfloat16*)X.q_x,
-                                           nr::nrc_rows_counted(&X.counters[0], cap, 0, 1), s->nrc_pred, c->num_sms, st);
+            const nr::NrcRows QR = nr::nrc_rows_counted(&X.counters[0], cap, 0, 1);
+            if (c->use_tc()) {
+                nr::nrc_launch_forward_tc_records(c->dev.wb_inf, c->dev.pinf, X.q_rec, QR, s->nrc_pred, c->num_sms,
+                                                  s->ps.counters + nr::CNT_ERR, st, c->tc_first_wait);
+            } else {
+                if (!s->nrc_qx) throw NrError(NR_ERR_DEVICE, "cache left the tensor cores during a render");
+                nr::nrc_launch_expand(X.q_rec, QR, s->nrc_qx, c->num_sms, st);
+                nr::nrc_launch_forward_inf(c->dev, s->nrc_qx, QR, s->nrc_pred, c->num_sms, st);
+                S.kernel_launches += 1;
+            }
             nr::launch_nrc_apply(s->ps, X, s->nrc_pred, cap, st);
             nr::launch_nrc_targets(s->ps, X, c->y, 1e3f, st);
             NR_CUDA(cudaMemsetAsync(c->loss, 0, 4, st));

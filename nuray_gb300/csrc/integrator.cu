@@ -374,8 +374,10 @@ __device__ __forceinline__ bool shade_one(const PathState& P, const DeviceScene&
             int q = warp_append(true, &C.counters[0]);
             C.q_slot[q] = slot;
             C.q_thr[q] = make_float4(T.x, T.y, T.z, 0.f);
-            nrc_encode(reinterpret_cast<uint32_t*>(C.q_x) + (size_t)q * 40, C.lo, C.inv_ext, hit_pos, wo, normal,
-                       nrc_roughness(M), M.c0);
+            uint32_t qr[8];
+            nrc_record(qr, C.lo, C.inv_ext, hit_pos, wo, normal, nrc_roughness(M), M.c0);
+            C.q_rec[2 * (size_t)q] = make_uint4(qr[0], qr[1], qr[2], qr[3]);
+            C.q_rec[2 * (size_t)q + 1] = make_uint4(qr[4], qr[5], qr[6], qr[7]);
             if (!C.direct) return false;
             query_here = true;  // the light sample below stays explicit
         } else if (train) {

@@ -6,6 +6,7 @@
 #include <cuda_bf16.h>
 
 #include "nr_device.cuh"
+#include "nrc_encode.cuh"
 
 namespace nr {
 
@@ -322,9 +323,7 @@ __device__ __forceinline__ f3 mat_sample(const MatView& M, RNG& s, f3 wo, f3 n) 
     }
 }
 
-// Cache input encoding, 80 values: position in the scene box with 12
-// frequencies of sin/cos per axis (72), outgoing direction and shading
-// normal as (phi / 2pi + 0.5, theta / pi) (4), roughness (1), albedo (3).
+// Cache input encoding: nrc_encode.cuh.
 __device__ __forceinline__ float nrc_roughness(const MatView& M) {
     if (M.type == NR_MAT_GGXR || M.type == NR_MAT_GGX) return M.alpha;
     if (M.type == NR_MAT_GLASS) return 0.f;
@@ -335,21 +334,14 @@ __device__ __forceinline__ bool nrc_diffuse(const MatView& M, float rough_min) {
     if (M.type == NR_MAT_GGXR || M.type == NR_MAT_GGX) return M.alpha >= rough_min;
     return false;
 }
-__device__ __forceinline__ void nrc_encode(uint32_t* dst, const float lo[3], const float inv_ext[3], f3 p, f3 wo, f3 n,
+// The cache's compact record of a vertex (nrc_encode.cuh): position in the
+// scene box, outgoing direction and shading normal as (phi / 2pi + 0.5,
+// theta / pi), roughness and albedo.
+__device__ __forceinline__ void nrc_record(uint32_t rec[8], const float lo[3], const float inv_ext[3], f3 p, f3 wo, f3 n,
                                            float rough, f3 albedo) {
-    float pp[3] = {(p.x - lo[0]) * inv_ext[0], (p.y - lo[1]) * inv_ext[1], (p.z - lo[2]) * inv_ext[2]};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float f = 1.f;
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-            float sv, cv;
-            sincospif(pp[a] * f, &sv, &cv);
-            __nv_bfloat162 v = __floats2bfloat162_rn(sv, cv);
-            dst[a * 12 + k] = *reinterpret_cast<uint32_t*>(&v);
-            f *= 2.f;
-        }
-    }
+    rec[0] = __float_as_uint((p.x - lo[0]) * inv_ext[0]);
+    rec[1] = __float_as_uint((p.y - lo[1]) * inv_ext[1]);
+    rec[2] = __float_as_uint((p.z - lo[2]) * inv_ext[2]);
     auto sph = [](f3 d, float& u, float& v) {
         u = atan2f(d.z, d.x) * (0.5f / 3.14159265f) + 0.5f;
         v = acosf(fminf(1.f, fmaxf(-1.f, d.y))) * (1.f / 3.14159265f);
@@ -359,10 +351,19 @@ __device__ __forceinline__ void nrc_encode(uint32_t* dst, const float lo[3], con
     sph(n, u1, v1);
     __nv_bfloat162 e0 = __floats2bfloat162_rn(u0, v0), e1 = __floats2bfloat162_rn(u1, v1);
     __nv_bfloat162 e2 = __floats2bfloat162_rn(rough, albedo.x), e3 = __floats2bfloat162_rn(albedo.y, albedo.z);
-    dst[36] = *reinterpret_cast<uint32_t*>(&e0);
-    dst[37] = *reinterpret_cast<uint32_t*>(&e1);
-    dst[38] = *reinterpret_cast<uint32_t*>(&e2);
-    dst[39] = *reinterpret_cast<uint32_t*>(&e3);
+    rec[3] = *reinterpret_cast<uint32_t*>(&e0);
+    rec[4] = *reinterpret_cast<uint32_t*>(&e1);
+    rec[5] = *reinterpret_cast<uint32_t*>(&e2);
+    rec[6] = *reinterpret_cast<uint32_t*>(&e3);
+    rec[7] = 0u;
+}
+// The full 160-byte encoding of a vertex (a training record); dst 16-byte aligned.
+__device__ __forceinline__ void nrc_encode(uint32_t* dst, const float lo[3], const float inv_ext[3], f3 p, f3 wo, f3 n,
+                                           float rough, f3 albedo) {
+    uint32_t rec[8], w[40];
+    nrc_record(rec, lo, inv_ext, p, wo, n, rough, albedo);
+    nrc_expand(rec, w);
+    nrc_store_row(dst, w);
 }
 
 // Camera::generateRay (src/scene/camera.cpp:24-32); film_h precomputed as

@@ -127,7 +127,7 @@ struct PathState {
 // Online neural radiance cache inside the wavefront (k_shade<true>): query
 // and training records written during shading, consumed after the batch.
 struct NrcCtx {
-    void* q_x;            // __nv_bfloat16 [cap][80] query encodings
+    uint4* q_rec;         // [cap][2] compact query records (nrc_encode.cuh)
     int32_t* q_slot;
     float4* q_thr;        // throughput at the query vertex
     void* t_x;            // __nv_bfloat16 [tcap][80] training encodings

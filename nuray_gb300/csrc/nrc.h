@@ -91,6 +91,13 @@ void nrc_tc_setup();
 void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
                            float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts = nullptr,
                            uint32_t first_wait = NR_TC_FIRST_WAIT_LIMIT);
+// The same over compact query records (nrc_encode.cuh, [rows][2]), expanded
+// in shared memory: 32 bytes read per row instead of 160.
+void nrc_launch_forward_tc_records(const __nv_bfloat16* wb, const float* params, const uint4* rec, const NrcRows& R,
+                                   float* out, int num_sms, uint32_t* err, cudaStream_t st,
+                                   uint32_t first_wait = NR_TC_FIRST_WAIT_LIMIT);
+// Compact records -> BF16 rows [rows][80] (for the mma.sync forward).
+void nrc_launch_expand(const uint4* rec, const NrcRows& R, __nv_bfloat16* x, int num_sms, cudaStream_t st);
 // After error bit 32 the process stops launching the tensor-core kernels
 // (their tensor memory may have been freed under running MMAs): every cache
 // falls back to the mma.sync kernels of nrc.cu.

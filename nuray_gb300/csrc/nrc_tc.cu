@@ -19,9 +19,11 @@
 // memory and returns.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "nrc.h"
+#include "nrc_encode.cuh"
 #include "nr_types.h"
 
 namespace nr {
@@ -156,10 +158,13 @@ __device__ __forceinline__ bool wg_sync_or(int id, bool v) {
 }
 }  // namespace
 
+// rec (or null): compact records [rows][2] (nrc_encode.cuh) expanded into
+// the A tile in place of rows of x.
 template <int NWG>
 __global__ void __launch_bounds__(128 * NWG) k_nrc_forward_tc(const __nv_bfloat16* __restrict__ wb,
                                                               const float* __restrict__ params,
-                                                              const __nv_bfloat16* __restrict__ x, NrcRows R,
+                                                              const __nv_bfloat16* __restrict__ x,
+                                                              const uint4* __restrict__ rec, NrcRows R,
                                                               float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
                                                               uint32_t* err, uint32_t first_wait) {
     int m0, M;
@@ -174,7 +179,8 @@ __global__ void __launch_bounds__(128 * NWG) k_nrc_forward_tc(const __nv_bfloat1
     }
     const int tiles = (M + TM - 1) / TM;
     if ((int)blockIdx.x * NWG >= tiles) return;  // no warpgroup of this CTA has a tile: no tensor memory taken
-    x += (size_t)m0 * IN;
+    if (rec) rec += 2 * (size_t)m0;
+    else x += (size_t)m0 * IN;
     out += (size_t)m0 * 3;
     const size_t LS = (size_t)R.ld * H;  // one layer of acts
 
@@ -224,11 +230,26 @@ __global__ void __launch_bounds__(128 * NWG) k_nrc_forward_tc(const __nv_bfloat1
         {  // input rows -> A (K = 80)
             const int r = wtid, row = tile * TM + r;
             unsigned char* dst = abuf + (r / 8) * (KC_IN * 128) + (r % 8) * 16;
+            if (rec) {
+                uint32_t w[40];
+                if (row < M) {
+                    const uint4 a = rec[2 * (size_t)row], b = rec[2 * (size_t)row + 1];
+                    const uint32_t q[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+                    nrc_expand(q, w);
+                } else {
 #pragma unroll
-            for (int c = 0; c < KC_IN; ++c) {
-                uint4 v = make_uint4(0u, 0u, 0u, 0u);
-                if (row < M) v = *reinterpret_cast<const uint4*>(x + (size_t)row * IN + 8 * c);
-                *reinterpret_cast<uint4*>(dst + c * 128) = v;
+                    for (int i = 0; i < 40; ++i) w[i] = 0u;
+                }
+#pragma unroll
+                for (int c = 0; c < KC_IN; ++c)
+                    *reinterpret_cast<uint4*>(dst + c * 128) = make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+            } else {
+#pragma unroll
+                for (int c = 0; c < KC_IN; ++c) {
+                    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                    if (row < M) v = *reinterpret_cast<const uint4*>(x + (size_t)row * IN + 8 * c);
+                    *reinterpret_cast<uint4*>(dst + c * 128) = v;
+                }
             }
         }
         for (int layer = 0; layer < 5; ++layer) {
@@ -508,9 +529,10 @@ void nrc_tc_setup() {
     cudaFuncSetAttribute(k_nrc_backward_data_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, BK_TOTAL);
 }
 
-void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
-                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts,
-                           uint32_t first_wait) {
+namespace {
+void launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const uint4* rec,
+                       const NrcRows& R, float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts,
+                       uint32_t first_wait) {
     const int M = R.count ? (R.n + R.steps - 1) / R.steps : R.n;
     if (M <= 0) return;
     const int tiles = (M + TM - 1) / TM;
@@ -518,8 +540,38 @@ void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const _
     // resident CTAs per SM by shared memory: 3 with one warpgroup (58 KB), 2 with two or three
     const int cap = num_sms * (kFwWg == 1 ? 3 : 2);
     if (blocks > cap) blocks = cap;
-    k_nrc_forward_tc<kFwWg><<<blocks, 128 * kFwWg, nrc_forward_tc_smem(), st>>>(wb, params, x, R, out, acts, err,
+    k_nrc_forward_tc<kFwWg><<<blocks, 128 * kFwWg, nrc_forward_tc_smem(), st>>>(wb, params, x, rec, R, out, acts, err,
                                                                               first_wait);
+}
+
+// Compact records -> BF16 rows of 80 (for the mma.sync forward).
+__global__ void k_nrc_expand(const uint4* __restrict__ rec, NrcRows R, __nv_bfloat16* __restrict__ x) {
+    const int total = R.count ? min((int)*R.count, R.n) : R.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint4 a = rec[2 * (size_t)i], b = rec[2 * (size_t)i + 1];
+        const uint32_t q[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t w[40];
+        nrc_expand(q, w);
+        nrc_store_row(reinterpret_cast<uint32_t*>(x + (size_t)i * IN), w);
+    }
+}
+}  // namespace
+
+void nrc_launch_forward_tc(const __nv_bfloat16* wb, const float* params, const __nv_bfloat16* x, const NrcRows& R,
+                           float* out, int num_sms, uint32_t* err, cudaStream_t st, __nv_bfloat16* acts,
+                           uint32_t first_wait) {
+    launch_forward_tc(wb, params, x, nullptr, R, out, num_sms, err, st, acts, first_wait);
+}
+
+void nrc_launch_forward_tc_records(const __nv_bfloat16* wb, const float* params, const uint4* rec, const NrcRows& R,
+                                   float* out, int num_sms, uint32_t* err, cudaStream_t st, uint32_t first_wait) {
+    launch_forward_tc(wb, params, nullptr, rec, R, out, num_sms, err, st, nullptr, first_wait);
+}
+
+void nrc_launch_expand(const uint4* rec, const NrcRows& R, __nv_bfloat16* x, int num_sms, cudaStream_t st) {
+    if (R.n <= 0) return;
+    const int blocks = std::min((R.n + 255) / 256, num_sms * 8);
+    k_nrc_expand<<<blocks, 256, 0, st>>>(rec, R, x);
 }
 
 size_t nrc_wt_image_bytes() { return (size_t)BK_A; }

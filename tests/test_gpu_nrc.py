@@ -211,6 +211,28 @@ def test_nrc_first_ends_paths_at_the_first_diffuse_vertex(gpu_lib):
     assert abs(img.mean() / ref.mean() - 1) < 0.15
 
 
+def test_render_queries_same_on_both_forward_kernels(gpu_lib):
+    """The render's cache queries go as compact records to the tensor-core
+    forward, which rebuilds the encoding in shared memory, and through an
+    expansion kernel to the mma.sync forward: two caches with the same
+    weights (learning rate 0: the frame's training steps leave them as they
+    are) give the same image up to the two forwards' FP32 accumulation
+    order."""
+    from nuray_gb300.nrc import Cache
+    S = cornell()
+    imgs = {}
+    for tc in (1, 0):
+        c = Cache(f"seed=5 tc={tc} lr=0")
+        c.attach(S)
+        p0 = c.get_params()
+        imgs[tc] = S.render(PARAMS + " nrc=1 nrc_first=1")
+        np.testing.assert_array_equal(c.get_params(), p0)
+    a, b = imgs[1], imgs[0]
+    assert np.all(np.isfinite(a)) and np.all(np.isfinite(b))
+    assert a.mean() > 0
+    np.testing.assert_allclose(a, b, rtol=2e-2, atol=2e-3)
+
+
 def test_tensor_core_forward_equals_mma_sync(gpu_lib):
     """The two inference kernels on the same BF16 weights and inputs: FP32
     accumulation in a different order, hidden activations rounded to BF16 by
