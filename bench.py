@@ -236,14 +236,16 @@ def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0, spf=64, 
         pt_curve, pt_t = C.progressive(S, p, 100000, ref, target, time_limit_s=limit_s, spf=k)
         nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "nrc_train=16384", limit_s, warmup=max(1, 256 // k),
                                      spf=k)
-        res_k = {"pt": C.summary(pt_curve, pt_t), "pt_nrc": C.summary(nrc_curve, nrc_t)}
+        res_k = {"pt": C.summary(pt_curve, pt_t, target), "pt_nrc": C.summary(nrc_curve, nrc_t, target)}
         if label:
             res_k["resolution"] = r
             out[label] = res_k
         else:
             out.update(res_k)
     out["note"] = ("GPU time (CUDA events) of the frames up to the first checkpoint at or below the target; "
-                   "'spp' is the samples per pixel at that checkpoint; None when not reached within the time limit")
+                   "'spp' is the samples per pixel at that checkpoint; None when not reached within the time limit; "
+                   "'ms_to_target_interp' interpolates the time of the crossing in log-log between the checkpoints "
+                   "on either side of it (checkpoints lie about 3 % apart in samples)")
     return out
 
 

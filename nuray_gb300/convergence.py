@@ -76,8 +76,25 @@ def run_nrc(scene, params, ref, target, frames, nrc_params, time_limit_s, warmup
         cache.close()
 
 
-def summary(curve, t):
-    return {"ms_to_target": None if t is None else round(t, 1), "spp": curve[-1][1], "final_relmse": curve[-1][2]}
+def crossing(curve, target):
+    """GPU time at which relMSE reaches `target`, interpolated in log-log
+    between the last checkpoint above it and the first at or below it (the
+    checkpoints lie a few percent apart in sample count); None when the
+    curve does not cross it."""
+    import math
+    for (t0, _, e0), (t1, _, e1) in zip(curve, curve[1:]):
+        if e0 > target >= e1 and e0 > 0 and e1 > 0 and t0 > 0:
+            if e0 == e1:
+                return t1
+            w = math.log(e0 / target) / math.log(e0 / e1)
+            return math.exp(math.log(t0) + w * (math.log(t1) - math.log(t0)))
+    return None
+
+
+def summary(curve, t, target=1e-3):
+    x = crossing(curve, target)
+    return {"ms_to_target": None if t is None else round(t, 1), "spp": curve[-1][1], "final_relmse": curve[-1][2],
+            "ms_to_target_interp": None if x is None else round(x, 1)}
 
 
 def compare(scene, params, target=1e-3, ref_spp=8192, frames=50000, nrc_params="nrc_train=16384", time_limit_s=60.0):
