@@ -365,7 +365,7 @@ int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, fl
  * BlinnPhong vertex, or GGX with roughness >= nrc_rough, default 0.05), at
  * vertex depth >= nrc_mindepth (default 1), with the cache's prediction, and
  * trains the cache online on the suffix radiance of nrc_train (default
- * 16384) training paths per wavefront batch in nrc_steps (default 2) Adam
+ * 16384) training paths per wavefront batch in nrc_steps (default 3) Adam
  * steps. Training paths end in the cache too, from vertex depth
  * nrc_train_depth on (default 3; 0 lets them run to the end), as the
  * reference's path_lim_train does (src/renderer/renderernrc.cpp:130). The

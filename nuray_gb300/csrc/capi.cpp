@@ -696,7 +696,7 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     a.nrc = c.get_int("nrc", nrc_mode ? 1 : 0) != 0;
     a.nrc_pre = nrc_mode && c.get_int("nrc_pre", 1) != 0;
     a.nrc_train = c.get_int("nrc_train", 16384);
-    a.nrc_steps = c.get_int("nrc_steps", 2);
+    a.nrc_steps = c.get_int("nrc_steps", 3);
     a.nrc_query = c.get_int("nrc_query", 1);
     a.nrc_first = nrc_mode ? 0 : (c.get_int("nrc_first", 0) != 0 ? 1 : 0);
     a.nrc_mindepth = nrc_mode ? c.get_int("path_lim", 2) : c.get_int("nrc_mindepth", a.nrc_first ? 0 : 1);
