@@ -234,7 +234,7 @@ def relmse_leg(S, params, res, target=1e-3, ref_spp=8192, limit_s=45.0, spf=64, 
             refs[r] = C.reference(S, p, ref_spp)
         ref = refs[r]
         pt_curve, pt_t = C.progressive(S, p, 100000, ref, target, time_limit_s=limit_s, spf=k)
-        nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "nrc_train=16384", limit_s, warmup=max(1, 256 // k),
+        nrc_curve, nrc_t = C.run_nrc(S, p, ref, target, 100000, "", limit_s, warmup=max(1, 256 // k),
                                      spf=k)
         res_k = {"pt": C.summary(pt_curve, pt_t, target), "pt_nrc": C.summary(nrc_curve, nrc_t, target)}
         if label:

@@ -97,7 +97,7 @@ def summary(curve, t, target=1e-3):
             "ms_to_target_interp": None if x is None else round(x, 1)}
 
 
-def compare(scene, params, target=1e-3, ref_spp=8192, frames=50000, nrc_params="nrc_train=16384", time_limit_s=60.0):
+def compare(scene, params, target=1e-3, ref_spp=8192, frames=50000, nrc_params="", time_limit_s=60.0):
     """Plain PT and PT + NRC against the same reference; returns both summaries and curves."""
     ref = reference(scene, params, ref_spp)
     pt_curve, pt_t = progressive(scene, params, frames, ref, target, time_limit_s=time_limit_s)

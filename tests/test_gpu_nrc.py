@@ -178,8 +178,8 @@ def test_nrc_render_close_to_reference(gpu_lib):
     c = Cache("seed=0 lr=3e-3")
     c.attach(S)
     for k in range(30):  # warm up the cache on training paths
-        S.render(PARAMS + f" nrc=1 nrc_query=0 nrc_train=3072 sample0={16 * k}")
-    img = S.render(PARAMS + " nrc=1 nrc_train=3072 sample0=1000")
+        S.render(PARAMS + f" nrc=1 nrc_query=0 nrc_train=3072 nrc_steps=2 sample0={16 * k}")
+    img = S.render(PARAMS + " nrc=1 nrc_train=3072 nrc_steps=2 sample0=1000")
     plain = S.render(PARAMS + " sample0=1000")
     rel = lambda a: float(np.mean((a - ref) ** 2 / (ref ** 2 + 1e-2)))
     print(f"relMSE at 16 spp: plain {rel(plain):.4f}, PT+NRC {rel(img):.4f}")
@@ -200,10 +200,10 @@ def test_nrc_first_ends_paths_at_the_first_diffuse_vertex(gpu_lib):
     c = Cache("seed=0 lr=3e-3")
     c.attach(S)
     for k in range(30):
-        S.render(PARAMS + f" nrc=1 nrc_query=0 nrc_train=3072 sample0={16 * k}")
-    S.render(PARAMS + " nrc=1 nrc_train=3072 sample0=1000")
+        S.render(PARAMS + f" nrc=1 nrc_query=0 nrc_train=3072 nrc_steps=2 sample0={16 * k}")
+    S.render(PARAMS + " nrc=1 nrc_train=3072 nrc_steps=2 sample0=1000")
     rays_default = S.stats()["rays"]
-    img = S.render(PARAMS + " nrc=1 nrc_train=3072 nrc_first=1 sample0=1000")
+    img = S.render(PARAMS + " nrc=1 nrc_train=3072 nrc_steps=2 nrc_first=1 sample0=1000")
     rays_first = S.stats()["rays"]
     print(f"extension rays: default {rays_default}, nrc_first {rays_first}; mean ratio {img.mean() / ref.mean():.3f}")
     assert np.all(np.isfinite(img)) and img.min() >= 0
