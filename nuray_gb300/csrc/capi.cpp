@@ -260,18 +260,13 @@ void upload_scene(nr_scene* s) {
     // then visits each node at most once and ends, and its stack holds at most
     // max_depth entries (checked against NR_STACK_LIMIT before the upload).
     {
-        std::vector<uint8_t> referenced(ng, 0);
-        auto check_child = [&](int parent, int r) {
-            if (r >= 0) {
-                if (r <= parent || r >= ng || referenced[r]++) throw NrError(NR_ERR_INVALID, "BVH is not a tree");
-            } else if (nr::leaf_first(r) < 0 || nr::leaf_first(r) + nr::leaf_count(r) > n) {
-                throw NrError(NR_ERR_INVALID, "BVH leaf outside the triangle array");
-            }
-        };
+        std::vector<int32_t> refs(2 * (size_t)ng);
         for (int i = 0; i < ng; ++i) {
-            check_child(i, gn[i].d.x);
-            check_child(i, gn[i].d.y);
+            refs[2 * (size_t)i] = gn[i].d.x;
+            refs[2 * (size_t)i + 1] = gn[i].d.y;
         }
+        const std::string bad = nr::check_tree_refs(refs.data(), ng, n);
+        if (!bad.empty()) throw NrError(NR_ERR_INVALID, bad);
     }
 
     // The same nodes with every child box widened by delta for the one-FMA

@@ -650,4 +650,21 @@ void build_bvh(const HostScene& s, Bvh& out, int threads) {
     root.reset();
 }
 
+std::string check_tree_refs(const int32_t* refs, int num_inner, int num_tris) {
+    std::vector<uint8_t> referenced((size_t)std::max(num_inner, 0), 0);
+    for (int i = 0; i < num_inner; ++i)
+        for (int side = 0; side < 2; ++side) {
+            const int32_t r = refs[2 * (size_t)i + side];
+            if (r >= 0) {
+                if (r <= i || r >= num_inner) return "BVH is not a tree: node " + std::to_string(i) + " refers to " + std::to_string(r);
+                if (referenced[r]++) return "BVH is not a tree: node " + std::to_string(r) + " has two parents";
+            } else {
+                const int32_t code = -1 - r, first = code >> 3, count = code & 7;
+                if ((int64_t)first + count > num_tris)
+                    return "BVH leaf outside the triangle array: node " + std::to_string(i);
+            }
+        }
+    return "";
+}
+
 }  // namespace nr

@@ -96,4 +96,12 @@ struct Bvh {
 };
 void build_bvh(const HostScene& s, Bvh& out, int threads);
 
+// The shape the device traversal relies on, checked on the child references
+// of the GPU node array (two per inner node: >= 0 an inner node, < 0 a leaf
+// -1 - ((first << 3) | count)): every inner node is the child of at most one
+// inner node, which has a smaller index, and every leaf's triangles lie in
+// [0, num_tris). A walk over such a tree visits each node at most once and
+// ends. Returns "" or what is wrong.
+std::string check_tree_refs(const int32_t* refs, int num_inner, int num_tris);
+
 }  // namespace nr

@@ -104,4 +104,13 @@ int shim_read_image(const char* path, int* w, int* h, float* rgb, char* err, int
     if (rgb) std::memcpy(rgb, v.data(), v.size() * sizeof(float));
     return 0;
 }
+
+// nr::check_tree_refs: 0 for a tree the traversal accepts, -1 with the message.
+int shim_check_tree(const int32_t* refs, int num_inner, int num_tris, char* err, int errlen) {
+    std::string e = nr::check_tree_refs(refs, num_inner, num_tris);
+    if (e.empty()) return 0;
+    std::strncpy(err, e.c_str(), (size_t)errlen - 1);
+    err[errlen - 1] = 0;
+    return -1;
+}
 }

@@ -34,6 +34,7 @@ def load():
     L.shim_png_encode.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
     L.shim_png_encode.restype = ctypes.c_long
     L.shim_read_image.argtypes = [ctypes.c_char_p, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
+    L.shim_check_tree.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
     return L
 
 

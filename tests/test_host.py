@@ -82,6 +82,53 @@ def test_bvh_builder_matches_reference_tree(host):
         np.testing.assert_array_equal(a, s[k])
 
 
+def _gpu_child_refs(kids, first, count):
+    """The child references of the GPU node array (capi.cpp upload_scene):
+    inner nodes numbered in depth-first order, leaves -1 - ((first << 3) | count)."""
+    inner = np.flatnonzero(kids[:, 0] >= 0)
+    index = -np.ones(len(kids), np.int64)
+    index[inner] = np.arange(len(inner))
+    ref = lambda c: int(index[c]) if kids[c, 0] >= 0 else -1 - ((int(first[c]) << 3) | int(count[c]))
+    return np.array([[ref(kids[i, 0]), ref(kids[i, 1])] for i in inner], np.int32)
+
+
+def _check_tree(host, refs, num_tris):
+    refs = np.ascontiguousarray(refs, np.int32)
+    err = ctypes.create_string_buffer(256)
+    rc = host.shim_check_tree(refs.ctypes.data, len(refs), num_tris, err, 256)
+    return rc, err.value.decode()
+
+
+def test_tree_check_admits_built_trees_and_refuses_malformed_ones(host):
+    """The closest-hit walk has no step budget: the upload refuses node arrays
+    in which a node has two parents, a child does not follow its parent, or a
+    leaf leaves the triangle array."""
+    sc = scenes.terrain_spheres(3, tiles=8, cells_per_tile=8, spheres=16, slices=12, stacks=8, lights=4,
+                                n_mats=4, extent=32.0)
+    box, kids, first, count, tris, depth = shim.bvh(host, sc["pos"])
+    n = len(sc["pos"])
+    refs = _gpu_child_refs(kids, first, count)
+    assert len(refs) > 100
+    assert _check_tree(host, refs, n) == (0, "")
+    inner = np.flatnonzero(refs[:, 0] >= 0)
+    i = int(inner[len(inner) // 2])
+    bad = refs.copy()
+    bad[i, 0] = i  # a cycle: a node as its own child
+    assert _check_tree(host, bad, n)[0] == -1
+    bad = refs.copy()
+    bad[i, 1] = bad[i, 0]  # one child referenced twice
+    rc, msg = _check_tree(host, bad, n)
+    assert rc == -1 and "two parents" in msg
+    bad = refs.copy()
+    bad[i + 1, 0] = i  # a child above its parent
+    assert _check_tree(host, bad, n)[0] == -1
+    bad = refs.copy()
+    bad[len(bad) - 1, 1] = -1 - (((n - 1) << 3) | 5)  # a leaf reaching past the last triangle
+    rc, msg = _check_tree(host, bad, n)
+    assert rc == -1 and "leaf" in msg
+    assert _check_tree(host, refs, n - 1)[0] == -1  # the same tree over fewer triangles
+
+
 def test_bvh_builder_parallel_is_deterministic(host, port_lib):
     from oracle.bind import Oracle
     sc = scenes.terrain_spheres(3, tiles=16, cells_per_tile=8, spheres=64, slices=16, stacks=12, lights=8,
