@@ -558,6 +558,14 @@ struct Builder {
                 if (cost < ans_cost) { ans_cost = cost; ans_mid = (int)i + 1; ans_axis = axis; }
             }
         }
+        // No cost below the start value (surface areas beyond the float range,
+        // about 1e19 units of extent): the reference would keep every triangle
+        // on one side and recurse until its stack overflows. A median split on
+        // the first axis instead, as the device builder does.
+        if (ans_mid == 0) {
+            ans_axis = 0;
+            ans_mid = (int)(n / 2);
+        }
         std::sort(prims.begin(), prims.end(), [ans_axis](const Key& a, const Key& b) { return a.k[ans_axis] < b.k[ans_axis]; });
         L.assign(prims.begin(), prims.begin() + ans_mid);
         R.assign(prims.begin() + ans_mid, prims.end());

@@ -98,3 +98,33 @@ def test_bad_option_is_an_error(gpu_lib):
     pos, mat, mats = soup(10, 0)
     with pytest.raises(Exception):
         Scene.from_arrays(pos, mat, mats, options="bvh=octree")
+
+
+def test_overflowing_surface_areas_build_and_intersect(gpu_lib):
+    """Nested triangles doubling in size up to 2^99 of extent: past about
+    2^64 the SAH's surface areas overflow float and no split has a finite
+    cost. Both builders split at the first axis's median there (the
+    reference would recurse without end) and give the same tree (distinct
+    keys); rays going up at (x, y) hit the smallest triangle that covers the
+    point, index ceil(log2(x + y))."""
+    from nuray_gb300 import Scene
+    n = 100
+    pos = np.array([[0, 0, 0.01 * k, 2.0 ** k, 0, 0.01 * k, 0, 2.0 ** k, 0.01 * k] for k in range(n)], np.float32)
+    mat = np.zeros(n, np.int32)
+    mats = [dict(type=0, c0=(0.5, 0.5, 0.5))]
+    H = Scene.from_arrays(pos, mat, mats)
+    G = Scene.from_arrays(pos, mat, mats, options="bvh=gpu")
+    for a, b in zip(tree(H), tree(G)):
+        np.testing.assert_array_equal(a, b)
+    rng = np.random.default_rng(0)
+    m = 4000
+    u = rng.integers(0, 41, m) + rng.uniform(0.1, 0.9, m)  # log2(x + y), away from the triangles' edges
+    f = rng.uniform(0.05, 0.95, m)
+    s = 2.0 ** u
+    o = np.stack([s * f, s * (1 - f), np.full(m, -1.0)], 1).astype(np.float32)
+    d = np.tile(np.float32([0, 0, 1]), (m, 1))
+    want = np.ceil(u).astype(np.int32)
+    for S in (H, G):
+        tri, t = S.intersect(o, d)[:2]
+        np.testing.assert_array_equal(tri, want)
+        np.testing.assert_allclose(t, 1.0 + 0.01 * want, rtol=1e-5)

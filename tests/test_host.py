@@ -129,6 +129,20 @@ def test_tree_check_admits_built_trees_and_refuses_malformed_ones(host):
     assert _check_tree(host, refs, n - 1)[0] == -1  # the same tree over fewer triangles
 
 
+def test_bvh_builder_survives_overflowing_surface_areas(host):
+    """Nested triangles doubling in size: past about 2^64 of extent the SAH's
+    surface areas overflow float and no split has a finite cost. The
+    reference's builder then keeps every triangle on one side and recurses
+    until its stack overflows; this one splits at the median of the first
+    axis, as the device builder does."""
+    n = 100
+    pos = np.array([[0, 0, 0.01 * k, 2.0 ** k, 0, 0.01 * k, 0, 2.0 ** k, 0.01 * k] for k in range(n)], np.float32)
+    box, kids, first, count, tris, depth = shim.bvh(host, pos)
+    assert sorted(tris.tolist()) == list(range(n))  # every triangle in exactly one leaf
+    assert count.max() <= 5 and depth < 40
+    assert _check_tree(host, _gpu_child_refs(kids, first, count), n) == (0, "")
+
+
 def test_bvh_builder_parallel_is_deterministic(host, port_lib):
     from oracle.bind import Oracle
     sc = scenes.terrain_spheres(3, tiles=16, cells_per_tile=8, spheres=64, slices=16, stacks=12, lights=8,
