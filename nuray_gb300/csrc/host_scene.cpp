@@ -193,14 +193,25 @@ std::string read_image(const std::string& path, int& w, int& h, std::vector<floa
         f.clear();
         f.seekg(0);
     }
+    // bytes left after the header: the pixel data must fit in them before
+    // anything is allocated for it
+    auto left = [&f]() -> uint64_t {
+        const std::streampos here = f.tellg();
+        if (here < 0) return 0;
+        f.seekg(0, std::ios::end);
+        const std::streampos end = f.tellg();
+        f.seekg(here);
+        return end > here ? (uint64_t)(end - here) : 0;
+    };
     std::string magic;
     f >> magic;
     if (magic == "PF" || magic == "Pf") {
         double scale;
         f >> w >> h >> scale;
         f.get();
-        if (w <= 0 || h <= 0) return "bad PFM header in " + path;
+        if (!f || w <= 0 || h <= 0) return "bad PFM header in " + path;
         int ch = magic == "PF" ? 3 : 1;
+        if ((uint64_t)w * (uint64_t)h * (uint64_t)ch * 4u > left()) return "truncated PFM " + path;
         std::vector<float> raw((size_t)w * h * ch);
         f.read(reinterpret_cast<char*>(raw.data()), raw.size() * sizeof(float));
         if (!f) return "truncated PFM " + path;
@@ -224,7 +235,8 @@ std::string read_image(const std::string& path, int& w, int& h, std::vector<floa
         int maxv;
         f >> w >> h >> maxv;
         f.get();
-        if (w <= 0 || h <= 0 || maxv != 255) return "unsupported PPM " + path;
+        if (!f || w <= 0 || h <= 0 || maxv != 255) return "unsupported PPM " + path;
+        if ((uint64_t)w * (uint64_t)h * 3u > left()) return "truncated PPM " + path;
         std::vector<unsigned char> raw((size_t)w * h * 3);
         f.read(reinterpret_cast<char*>(raw.data()), raw.size());
         if (!f) return "truncated PPM " + path;

@@ -91,11 +91,15 @@ const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 
 // RFC 1951 3.2.7: order of the code-length code lengths.
 const uint8_t kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
-std::string inflate_codes(Bits& b, const Code& lit, const Code& dist, std::vector<uint8_t>& out) {
+std::string inflate_codes(Bits& b, const Code& lit, const Code& dist, std::vector<uint8_t>& out, size_t limit) {
     while (true) {
         int s = decode(b, lit);
         if (s < 0 || b.over) return "corrupt deflate data (literal/length code)";
-        if (s < 256) { out.push_back((uint8_t)s); continue; }
+        if (s < 256) {
+            if (out.size() >= limit) return "deflate data longer than expected";
+            out.push_back((uint8_t)s);
+            continue;
+        }
         if (s == 256) return "";
         s -= 257;
         if (s >= 29) return "corrupt deflate data (length symbol)";
@@ -104,12 +108,13 @@ std::string inflate_codes(Bits& b, const Code& lit, const Code& dist, std::vecto
         if (ds < 0 || ds >= 30 || b.over) return "corrupt deflate data (distance code)";
         size_t d = kDistBase[ds] + b.take(kDistExtra[ds]);
         if (d > out.size()) return "corrupt deflate data (distance beyond output)";
+        if (len > limit - out.size()) return "deflate data longer than expected";
         size_t from = out.size() - d;
         for (size_t i = 0; i < len; ++i) out.push_back(out[from + i]);  // overlapping copies repeat
     }
 }
 
-std::string inflate_raw(Bits& b, std::vector<uint8_t>& out) {
+std::string inflate_raw(Bits& b, std::vector<uint8_t>& out, size_t limit) {
     bool last = false;
     while (!last) {
         last = b.take(1) != 0;
@@ -119,6 +124,7 @@ std::string inflate_raw(Bits& b, std::vector<uint8_t>& out) {
             b.align();
             uint32_t len = b.take(16), nlen = b.take(16);
             if (b.over || (len ^ 0xffffu) != nlen) return "corrupt stored block";
+            if (len > limit - out.size()) return "deflate data longer than expected";
             for (uint32_t i = 0; i < len; ++i) out.push_back((uint8_t)b.take(8));
             if (b.over) return "truncated stored block";
         } else if (type == 1) {  // fixed Huffman codes (RFC 1951 3.2.6)
@@ -139,7 +145,7 @@ std::string inflate_raw(Bits& b, std::vector<uint8_t>& out) {
                 build(c, l, 30);
                 return c;
             }();
-            std::string e = inflate_codes(b, lit, dist, out);
+            std::string e = inflate_codes(b, lit, dist, out, limit);
             if (!e.empty()) return e;
         } else if (type == 2) {  // dynamic Huffman codes (RFC 1951 3.2.7)
             const int hlit = (int)b.take(5) + 257, hdist = (int)b.take(5) + 1, hclen = (int)b.take(4) + 4;
@@ -171,7 +177,7 @@ std::string inflate_raw(Bits& b, std::vector<uint8_t>& out) {
             if (lens[256] == 0) return "no end-of-block code";
             Code lit, dist;
             if (!build(lit, lens, hlit) || !build(dist, lens + hlit, hdist)) return "corrupt Huffman lengths";
-            std::string e = inflate_codes(b, lit, dist, out);
+            std::string e = inflate_codes(b, lit, dist, out, limit);
             if (!e.empty()) return e;
         } else {
             return "reserved deflate block type";
@@ -217,7 +223,7 @@ uint32_t crc32_png(const uint8_t* p, size_t n, uint32_t crc) {
     return ~crc;
 }
 
-std::string zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>& out) {
+std::string zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>& out, size_t limit) {
     if (n < 6) return "zlib stream too short";
     const uint8_t cmf = data[0], flg = data[1];
     if ((cmf & 0x0f) != 8 || (cmf >> 4) > 7) return "not a deflate zlib stream";
@@ -225,7 +231,7 @@ std::string zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>& ou
     if (flg & 0x20) return "zlib preset dictionary not supported";
     Bits b(data + 2, n - 2);
     out.clear();
-    std::string e = inflate_raw(b, out);
+    std::string e = inflate_raw(b, out, limit);
     if (!e.empty()) return e;
     b.align();
     const size_t used = 2 + b.pos - (size_t)(b.cnt / 8);
@@ -286,9 +292,25 @@ std::string png_decode(const std::vector<uint8_t>& f, int& width, int& height, s
                           ((ctype == 2 || ctype == 4 || ctype == 6) && (depth == 8 || depth == 16));
     if (!depth_ok) return "bad PNG bit depth for its colour type";
     if (ctype == 3 && (palette.empty() || palette.size() % 3 != 0)) return "palette image without PLTE";
+    // The filtered rows' size, from the header: the inflater stops past it
+    // (a small stream cannot expand without bound), and the image is only
+    // allocated once all of its rows are there.
+    uint64_t need = 0;
+    {
+        static const uint32_t a7[7][4] = {{0, 0, 8, 8}, {4, 0, 8, 8}, {0, 4, 4, 8}, {2, 0, 4, 4},
+                                          {0, 2, 2, 4}, {1, 0, 2, 2}, {0, 1, 1, 2}};
+        for (int p = 0; p < (interlace ? 7 : 1); ++p) {
+            const uint32_t x0 = interlace ? a7[p][0] : 0, y0 = interlace ? a7[p][1] : 0;
+            const uint32_t dx = interlace ? a7[p][2] : 1, dy = interlace ? a7[p][3] : 1;
+            if (x0 >= w || y0 >= h) continue;
+            const uint64_t pw = (w - x0 + dx - 1) / dx, ph = (h - y0 + dy - 1) / dy;
+            need += ph * (1 + (pw * channels * depth + 7) / 8);
+        }
+    }
     std::vector<uint8_t> raw;
-    std::string e = zlib_inflate(idat.data(), idat.size(), raw);
+    std::string e = zlib_inflate(idat.data(), idat.size(), raw, (size_t)need + 65536);
     if (!e.empty()) return e;
+    if (raw.size() < need) return "truncated PNG image data";
 
     const int bpp = (channels * depth + 7) / 8;  // filter byte distance
     rgba.assign((size_t)w * h * 4, 0);

@@ -26,8 +26,9 @@ std::string png_decode(const std::vector<uint8_t>& file, int& width, int& height
 // the top. Returns an empty string on success or an error message.
 std::string jpeg_decode(const std::vector<uint8_t>& file, int& width, int& height, std::vector<uint8_t>& rgb);
 
-// zlib stream -> bytes (exposed for tests). Returns "" or an error message.
-std::string zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>& out);
+// zlib stream -> bytes (exposed for tests), at most `limit` of them.
+// Returns "" or an error message.
+std::string zlib_inflate(const uint8_t* data, size_t n, std::vector<uint8_t>& out, size_t limit = (size_t)-1);
 
 // 8-bit RGB image (row 0 at the top) -> PNG file bytes (colour type 2,
 // filter 0, DEFLATE stored blocks).

@@ -236,15 +236,22 @@ struct Decoder {
             hmax = std::max(hmax, c.h);
             vmax = std::max(vmax, c.v);
         }
+        // At most 2^28 pixels (16384 x 16384), and the coefficient planes are
+        // only allocated when the file can hold them: every coded block
+        // takes at least one bit of entropy-coded data.
+        if ((uint64_t)width * (uint64_t)height > (1ull << 28)) throw JError{"JPEG larger than 2^28 pixels"};
         mcux = (width + 8 * hmax - 1) / (8 * hmax);
         mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+        uint64_t coded_blocks = 0;
         for (auto& c : comps) {
             c.bw = mcux * c.h;
             c.bh = mcuy * c.v;
             c.cbw = ((width * c.h + hmax - 1) / hmax + 7) / 8;
             c.cbh = ((height * c.v + vmax - 1) / vmax + 7) / 8;
-            c.coef.assign((size_t)c.bw * c.bh * 64, 0);
+            coded_blocks += (uint64_t)c.cbw * c.cbh;
         }
+        if (coded_blocks > 8 * (uint64_t)(n - pos)) throw JError{"JPEG data too short for its frame size"};
+        for (auto& c : comps) c.coef.assign((size_t)c.bw * c.bh * 64, 0);
         have_frame = true;
     }
 

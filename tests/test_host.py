@@ -143,6 +143,42 @@ def test_bvh_builder_survives_overflowing_surface_areas(host):
     assert _check_tree(host, _gpu_child_refs(kids, first, count), n) == (0, "")
 
 
+def test_image_headers_promising_more_than_the_file_holds_are_refused(host, tmp_path):
+    """Declared sizes are checked against the data before anything is
+    allocated for the pixels: PPM and PFM against the bytes left in the
+    file, PNG against the inflated rows (and the inflater stops past them),
+    JPEG against a 2^28-pixel cap and one bit of scan data per coded block."""
+    import struct
+    import zlib
+    import jpeg_enc
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xffffffff)
+
+    def png(w, h, idat):
+        return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+                + chunk(b"IDAT", idat) + chunk(b"IEND", b""))
+
+    for name, data, msg in (("a.ppm", b"P6\n99999999 99999999\n255\n" + bytes(30), "truncated PPM"),
+                            ("b.pfm", b"PF\n99999 99999\n-1.0\n" + bytes(30), "truncated PFM")):
+        (tmp_path / name).write_bytes(data)
+        with pytest.raises(ValueError, match=msg):
+            shim.read_image(host, str(tmp_path / name))
+    with pytest.raises(ValueError, match="truncated PNG image data"):
+        shim.png_decode(host, png(30000, 30000, zlib.compress(b"\0" * 100)))
+    with pytest.raises(ValueError, match="longer than expected"):  # 10 MB of rows for a 64 x 64 image
+        shim.png_decode(host, png(64, 64, zlib.compress(b"\0" * 10_000_000, 9)))
+    img = (np.random.default_rng(0).random((8, 8, 3)) * 255).astype(np.uint8)
+    base = bytearray(jpeg_enc.encode(img)[0])
+    i = base.find(b"\xff\xc0")
+    for side, msg in ((65535, "larger than 2"), (16000, "too short for its frame size")):
+        b = bytearray(base)
+        b[i + 5:i + 7] = side.to_bytes(2, "big")
+        b[i + 7:i + 9] = side.to_bytes(2, "big")
+        with pytest.raises(ValueError, match=msg):
+            shim.jpeg_decode(host, bytes(b))
+
+
 def test_bvh_builder_parallel_is_deterministic(host, port_lib):
     from oracle.bind import Oracle
     sc = scenes.terrain_spheres(3, tiles=16, cells_per_tile=8, spheres=64, slices=16, stacks=12, lights=8,
