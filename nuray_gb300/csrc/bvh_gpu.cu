@@ -222,14 +222,22 @@ inline unsigned blocks(long n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
 
-std::string build_bvh_gpu(const float* pos_host, int n, Bvh& out, cudaStream_t st, double* device_ms) {
+std::string build_bvh_gpu(const float* pos_host, int n, Bvh& out, cudaStream_t st, double* device_ms,
+                          int depth_limit) {
     out = Bvh{};
     if (n <= 0) return "";
     try {
         Scratch S;
-        cudaEvent_t e0, e1;
-        check(cudaEventCreate(&e0));
-        check(cudaEventCreate(&e1));
+        struct Events {  // destroyed on every way out
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            ~Events() {
+                if (e0) cudaEventDestroy(e0);
+                if (e1) cudaEventDestroy(e1);
+            }
+        } ev;
+        check(cudaEventCreate(&ev.e0));
+        check(cudaEventCreate(&ev.e1));
+        cudaEvent_t e0 = ev.e0, e1 = ev.e1;
         float* pos = S.get<float>(9 * (size_t)n);
         check(cudaMemcpyAsync(pos, pos_host, 9 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
         check(cudaEventRecord(e0, st));
@@ -283,6 +291,12 @@ std::string build_bvh_gpu(const float* pos_host, int n, Bvh& out, cudaStream_t s
         int n0 = 0, n1 = 1, levels = 0;
         while (n0 < n1) {
             if (++levels > n + 1) throw std::string("BVH build did not terminate");
+            if (levels > depth_limit + 1) {  // the tree would be refused by the traversal's stack
+                check(cudaStreamSynchronize(st));  // nothing of the build in flight when its buffers go
+                out = Bvh{};
+                out.max_depth = depth_limit + 1;
+                return "";
+            }
             const unsigned nb = blocks(n1 - n0);
             for (int a = 0; a < 3; ++a) {
                 k_items<<<blocks(n), 256, 0, st>>>(lists[a], seg, pmin, pmax, n, 0, items);
@@ -331,8 +345,6 @@ std::string build_bvh_gpu(const float* pos_host, int n, Bvh& out, cudaStream_t s
             check(cudaEventElapsedTime(&ms, e0, e1));
             *device_ms = ms;
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
 
         // depth-first, left child first (the layout build_bvh produces)
         out.nodes.reserve(nn);

@@ -17,7 +17,9 @@ namespace nr {
 // the reference's tree; among equal keys the order here is stable (by
 // loader index) while the reference's std::sort leaves it unspecified, so
 // trees of such scenes can differ (the closest hits differ only on exact
-// ties). Returns "" or an error message.
-std::string build_bvh_gpu(const float* pos, int n, Bvh& out, cudaStream_t st, double* device_ms = nullptr);
+// ties). Past depth_limit it stops as build_bvh does (no nodes, max_depth =
+// depth_limit + 1). Returns "" or an error message.
+std::string build_bvh_gpu(const float* pos, int n, Bvh& out, cudaStream_t st, double* device_ms = nullptr,
+                          int depth_limit = 2048);
 
 }  // namespace nr

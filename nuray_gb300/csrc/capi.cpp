@@ -422,16 +422,21 @@ void finish_scene(nr_scene* s, const char* options) {
     NR_CUDA(cudaMallocHost(&s->counters_host, nr::NUM_COUNTERS * sizeof(uint32_t)));
     auto t0 = std::chrono::steady_clock::now();
     s->bvh_device_ms = 0.0;
+    // the deepest tree the traversal stacks hold; the builders stop past it
+    const int depth_limit = NR_STACK_LIMIT - 2;
     if (bvh == "gpu") {
-        std::string err = nr::build_bvh_gpu(s->host.pos.data(), s->host.num_tris(), s->bvh, s->stream, &s->bvh_device_ms);
+        std::string err = nr::build_bvh_gpu(s->host.pos.data(), s->host.num_tris(), s->bvh, s->stream, &s->bvh_device_ms,
+                                            depth_limit);
         if (!err.empty()) throw NrError(NR_ERR_CUDA, err);
     } else {
         int threads = (int)std::max(1u, std::thread::hardware_concurrency());
-        nr::build_bvh(s->host, s->bvh, threads);
+        nr::build_bvh(s->host, s->bvh, threads, depth_limit);
     }
     s->bvh_wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (s->bvh.max_depth + 2 > NR_STACK_LIMIT)
-        throw NrError(NR_ERR_INVALID, "BVH depth " + std::to_string(s->bvh.max_depth) + " exceeds the traversal stack");
+    if (s->bvh.max_depth > depth_limit)
+        throw NrError(NR_ERR_INVALID, "BVH deeper than " + std::to_string(depth_limit) +
+                                          " levels (the traversal stack's limit; many coincident triangles make "
+                                          "the reference's SAH split them off one by one)");
     nr::launch_setup(s->num_sms);
     upload_scene(s);
     // the static scratch of nr_intersect_noalloc: reserved and located on

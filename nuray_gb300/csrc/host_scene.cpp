@@ -534,6 +534,8 @@ struct Builder {
     const std::vector<float>* pmax;
     const std::vector<float>* pos;
     std::atomic<int> spare_threads{0};
+    int depth_limit = 0;
+    std::atomic<bool> too_deep{false};
 
     static inline float fmn(float a, float b) { return (b < a) ? b : a; }  // std::min
     static inline float fmx(float a, float b) { return (a < b) ? b : a; }  // std::max
@@ -583,8 +585,13 @@ struct Builder {
         R.assign(prims.begin() + ans_mid, prims.end());
     }
 
-    std::unique_ptr<TmpNode> build(std::vector<Key>& prims) {
+    std::unique_ptr<TmpNode> build(std::vector<Key>& prims, int depth) {
         auto node = std::make_unique<TmpNode>();
+        // past the depth limit the tree is refused whole; stop descending
+        if (depth > depth_limit || too_deep.load(std::memory_order_relaxed)) {
+            too_deep = true;
+            return node;
+        }
         if (prims.size() <= 5) {  // BVH::_build leaf rule (src/hierarchy/bvh.cpp:62-65)
             for (int k = 0; k < 3; ++k) { node->lo[k] = 1e18f; node->hi[k] = -1e18f; }
             const float* P = pos->data();
@@ -603,13 +610,13 @@ struct Builder {
         split(prims, L, R);
         std::vector<Key>().swap(prims);
         if (L.size() + R.size() > 20000 && spare_threads.fetch_sub(1) > 0) {
-            auto fut = std::async(std::launch::async, [&]() { return build(L); });
-            node->r = build(R);
+            auto fut = std::async(std::launch::async, [&]() { return build(L, depth + 1); });
+            node->r = build(R, depth + 1);
             node->l = fut.get();
             spare_threads.fetch_add(1);
         } else {
-            node->l = build(L);
-            node->r = build(R);
+            node->l = build(L, depth + 1);
+            node->r = build(R, depth + 1);
         }
         for (int k = 0; k < 3; ++k) {
             node->lo[k] = fmn(node->l->lo[k], node->r->lo[k]);
@@ -643,7 +650,7 @@ void flatten(const TmpNode* t, int depth, Bvh& out) {
 
 }  // namespace
 
-void build_bvh(const HostScene& s, Bvh& out, int threads) {
+void build_bvh(const HostScene& s, Bvh& out, int threads, int depth_limit) {
     const int n = s.num_tris();
     std::vector<float> pmin(3 * (size_t)n), pmax(3 * (size_t)n);
     std::vector<Key> prims(n);
@@ -662,8 +669,13 @@ void build_bvh(const HostScene& s, Bvh& out, int threads) {
     Builder b;
     b.pmin = &pmin; b.pmax = &pmax; b.pos = &s.pos;
     b.spare_threads = threads > 1 ? threads - 1 : 0;
-    std::unique_ptr<TmpNode> root = b.build(prims);
+    b.depth_limit = depth_limit;
+    std::unique_ptr<TmpNode> root = b.build(prims, 0);
     out = Bvh();
+    if (b.too_deep) {  // no tree; the depth says why
+        out.max_depth = depth_limit + 1;
+        return;
+    }
     out.nodes.reserve(n > 0 ? (size_t)n : 1);
     flatten(root.get(), 0, out);
     // free the temporary tree iteratively-deep recursion is bounded by depth

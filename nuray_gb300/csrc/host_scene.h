@@ -94,7 +94,10 @@ struct Bvh {
     std::vector<int32_t> leaf_tris;  // triangle indices (loader order), leaves depth-first
     int32_t max_depth = 0;
 };
-void build_bvh(const HostScene& s, Bvh& out, int threads);
+// Stops past depth_limit (the tree would be refused by the traversal's
+// stack) and returns no nodes with max_depth = depth_limit + 1, instead of
+// recursing as deep as the scene asks (identical triangles make a chain).
+void build_bvh(const HostScene& s, Bvh& out, int threads, int depth_limit = 2048);
 
 // The shape the device traversal relies on, checked on the child references
 // of the GPU node array (two per inner node: >= 0 an inner node, < 0 a leaf

@@ -12,12 +12,12 @@ extern "C" {
 // BVH over n triangles (pos: 9 floats each). Returns the node count; arrays
 // as nr_bvh_export. Call with null buffers to size them.
 int shim_bvh(int n, const float* pos, float* box, int* kids, int* first, int* count, int* tris, int* n_tris,
-             int* depth, int threads) {
+             int* depth, int threads, int depth_limit) {
     nr::HostScene s;
     s.pos.assign(pos, pos + 9 * (size_t)n);
     s.mat.assign(n, 0);
     nr::Bvh b;
-    nr::build_bvh(s, b, threads);
+    nr::build_bvh(s, b, threads, depth_limit);
     for (size_t i = 0; i < b.nodes.size(); ++i) {
         const nr::BvhNode& x = b.nodes[i];
         if (box) for (int k = 0; k < 3; ++k) { box[6 * i + k] = x.lo[k]; box[6 * i + 3 + k] = x.hi[k]; }

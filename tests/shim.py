@@ -22,7 +22,7 @@ def load():
                         os.path.join(ROOT, "include"), *srcs, "-o", LIB, "-lpthread"], check=True)
     L = ctypes.CDLL(LIB)
     vp = ctypes.c_void_p
-    L.shim_bvh.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int]
+    L.shim_bvh.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int]
     L.shim_load.argtypes = [ctypes.c_char_p, vp, vp, vp, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
     L.shim_config_int.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
     L.shim_config_float.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_float]
@@ -79,18 +79,19 @@ def read_image(L, path):
     return out
 
 
-def bvh(L, pos, threads=4):
+def bvh(L, pos, threads=4, depth_limit=2048):
     pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 9)
     n = pos.shape[0]
     nt, dep = ctypes.c_int(), ctypes.c_int()
-    nn = L.shim_bvh(n, pos.ctypes.data, None, None, None, None, None, ctypes.byref(nt), ctypes.byref(dep), threads)
+    nn = L.shim_bvh(n, pos.ctypes.data, None, None, None, None, None, ctypes.byref(nt), ctypes.byref(dep), threads,
+                    depth_limit)
     box = np.zeros((nn, 6), np.float32)
     kids = np.zeros((nn, 2), np.int32)
     first = np.zeros(nn, np.int32)
     count = np.zeros(nn, np.int32)
     tris = np.zeros(nt.value, np.int32)
     L.shim_bvh(n, pos.ctypes.data, box.ctypes.data, kids.ctypes.data, first.ctypes.data, count.ctypes.data,
-               tris.ctypes.data, ctypes.byref(nt), ctypes.byref(dep), threads)
+               tris.ctypes.data, ctypes.byref(nt), ctypes.byref(dep), threads, depth_limit)
     return box, kids, first, count, tris, dep.value
 
 

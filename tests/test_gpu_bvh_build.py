@@ -128,3 +128,21 @@ def test_overflowing_surface_areas_build_and_intersect(gpu_lib):
         tri, t = S.intersect(o, d)[:2]
         np.testing.assert_array_equal(tri, want)
         np.testing.assert_allclose(t, 1.0 + 0.01 * want, rtol=1e-5)
+
+
+def test_coincident_triangles_are_refused_at_the_depth_limit(gpu_lib):
+    """20,000 coincident triangles: every split costs the same, the
+    reference's SAH peels one off per level, and the chain is deeper than
+    the traversal stack holds. Both builders stop at that limit and the
+    scene is refused, instead of building (or recursing) 20,000 levels."""
+    from nuray_gb300 import Scene
+    from nuray_gb300._lib import NuRayError
+    n = 20000
+    pos = np.tile(np.float32([0, 0, 0, 1, 0, 0, 0, 1, 0]), (n, 1))
+    for opts in ("", "bvh=gpu"):
+        with pytest.raises(NuRayError, match="deeper than 94 levels"):
+            Scene.from_arrays(pos, np.zeros(n, np.int32), [dict(type=0, c0=(0.5, 0.5, 0.5))], options=opts)
+    # the device stays usable
+    S = Scene.from_arrays(pos[:50], np.zeros(50, np.int32), [dict(type=0, c0=(0.5, 0.5, 0.5))], options="bvh=gpu")
+    tri = S.intersect(np.float32([[0.2, 0.2, 1.0]]), np.float32([[0, 0, -1]]))[0]
+    assert 0 <= tri[0] < 50

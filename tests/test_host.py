@@ -143,6 +143,21 @@ def test_bvh_builder_survives_overflowing_surface_areas(host):
     assert _check_tree(host, _gpu_child_refs(kids, first, count), n) == (0, "")
 
 
+def test_bvh_builder_stops_at_its_depth_limit(host):
+    """Coincident triangles give every split the same cost, so the reference's
+    SAH peels one off per level: a chain as deep as the triangle count. The
+    builder stops past its depth limit (the traversal stack's, at scene
+    creation) and returns no nodes with max_depth = limit + 1, instead of
+    recursing until the host stack overflows (100,000 of them did)."""
+    pos = np.tile(np.float32([0, 0, 0, 1, 0, 0, 0, 1, 0]), (100000, 1))
+    box, kids, first, count, tris, depth = shim.bvh(host, pos, depth_limit=94)
+    assert depth == 95 and len(kids) == 0
+    box, kids, first, count, tris, depth = shim.bvh(host, pos[:300], depth_limit=94)
+    assert depth == 95 and len(kids) == 0  # a chain of 295 levels is past the limit too
+    box, kids, first, count, tris, depth = shim.bvh(host, pos[:60], depth_limit=94)
+    assert depth == 55 and len(kids) == 2 * 55 + 1  # a chain within the limit is built whole
+
+
 def test_image_headers_promising_more_than_the_file_holds_are_refused(host, tmp_path):
     """Declared sizes are checked against the data before anything is
     allocated for the pixels: PPM and PFM against the bytes left in the
