@@ -728,6 +728,17 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     if (a.wave <= 0) throw NrError(NR_ERR_INVALID, "wave must be positive");
     if (a.pol.maxdepth < 0 || a.pol.rrdepth < 0) throw NrError(NR_ERR_INVALID, "rrdepth and maxdepth must be >= 0");
     a.cam = cam ? *cam : nr::camera_from_config(c);
+    // a camera the film cannot be built from: every ray would be NaN (the
+    // reference checks nothing and renders black or garbage)
+    {
+        const nr_camera& k = a.cam;
+        const float v[11] = {k.pos[0], k.pos[1], k.pos[2], k.gaze[0], k.gaze[1], k.gaze[2],
+                             k.up[0], k.up[1], k.up[2], k.fov, k.aspect};
+        for (float x : v)
+            if (!std::isfinite(x)) throw NrError(NR_ERR_INVALID, "camera with a non-finite value");
+        if (!(k.fov > 0.0f && k.fov < 180.0f)) throw NrError(NR_ERR_INVALID, "camera fov must lie in (0, 180) degrees");
+        if (!(k.aspect > 0.0f)) throw NrError(NR_ERR_INVALID, "camera aspect must be positive");
+    }
     return a;
 }
 

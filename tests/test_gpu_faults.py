@@ -39,3 +39,24 @@ def test_render_over_the_cap_fails_and_the_scene_stays_usable(gpu_lib):
     # the same frame fits in waves small enough for the cap
     big = SMALL.replace("imgw=64 imgh=48", "imgw=320 imgh=240")
     np.testing.assert_array_equal(S.render(big + " wave=65536"), free.render(big))
+
+
+def test_cameras_without_a_film_are_refused(gpu_lib):
+    """A camera with a non-finite value, a field of view outside (0, 180)
+    degrees or a non-positive aspect would make every ray NaN: the call is
+    refused with NR_ERR_INVALID and the scene renders normally afterwards."""
+    from nuray_gb300._lib import NuRayError, camera_from_params
+    S = _scene()
+    for bad in ("camfov=0", "camfov=180", "camfov=-5", "camasp=0", "camasp=-1"):
+        with pytest.raises(NuRayError, match="NR_ERR_INVALID"):
+            S.render(SMALL.replace("camfov=64", "").replace("camasp=1.333", "") + " " + bad)
+    cam = camera_from_params(SMALL)
+    cam.pos[1] = float("nan")
+    with pytest.raises(NuRayError, match="non-finite"):
+        S.render(SMALL, camera=cam)
+    cam = camera_from_params(SMALL)
+    cam.fov = float("inf")
+    with pytest.raises(NuRayError, match="NR_ERR_INVALID"):
+        S.render(SMALL, camera=cam)
+    img = S.render(SMALL)
+    assert np.all(np.isfinite(img)) and img.mean() > 0
