@@ -547,8 +547,17 @@ static void launch_shade(const PathState& P, const DeviceScene& S, const Policy&
 #ifndef NR_TAIL_MAX_BOUNCES
 #define NR_TAIL_MAX_BOUNCES 4096
 #endif
+// Resident blocks per SM requested for the tail kernel. Its paths wait on
+// dependent traversal loads with few live lanes, so warps in flight pay more
+// than the registers' spills cost: 960x540 frames of 1 spp take 1.543 ms at 4
+// blocks (89 registers), 1.536 at 6, 1.463 at 8 (64 registers, 176 bytes
+// spilled), 1.459 at 10, 1.476 at 12 and 1.535 at 16 (40 and 32 registers,
+// kilobytes spilled).
+#ifndef NR_TAIL_MINB
+#define NR_TAIL_MINB 8
+#endif
 template <bool NRC, bool FAST>
-__global__ void __launch_bounds__(128, 4) k_tail(PathState P, DeviceScene S, Policy pol, NrcCtx C) {
+__global__ void __launch_bounds__(128, NR_TAIL_MINB) k_tail(PathState P, DeviceScene S, Policy pol, NrcCtx C) {
     const uint32_t n = P.counters[CNT_IN];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
