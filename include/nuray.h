@@ -192,6 +192,32 @@ int nr_scene_build_times(const nr_scene* scene, double* bvh_wall_ms, double* bvh
  * be NULL. */
 int nr_scene_export(const nr_scene* scene, float* pos, float* uv, float* nrm, int32_t* mat, nr_material* mats);
 
+/* A tree for nr_scene_create_bvh, in the layout nr_bvh_export writes:
+ * num_nodes nodes, node 0 the root, every child after its parent (depth-first
+ * order, as exported, is one such order); box[6] per node (min, max);
+ * kids[2] per node, -1, -1 for a leaf; a leaf's leaf_first / leaf_count
+ * (at most 7) into leaf_tris, the num_tris triangle indices (loader order)
+ * in leaf order. Closest-hit ties between leaves go to the larger
+ * leaf_first, which is the reference's "later leaf in depth-first order"
+ * when the leaves are laid out depth-first, as the reference's are. */
+typedef struct nr_bvh {
+    int32_t num_nodes;
+    const float* box;
+    const int32_t* kids;
+    const int32_t* leaf_first;
+    const int32_t* leaf_count;
+    const int32_t* leaf_tris;
+} nr_bvh;
+
+/* nr_scene_create_opts with the caller's tree instead of a build (the
+ * reference's BVH built by BVH::build, src/hierarchy/bvh.cpp:60-70, handed
+ * over, or a tree exported earlier). Refused with NR_ERR_INVALID unless
+ * leaf_tris is a permutation of the triangles, the leaves partition it,
+ * every node but the root has exactly one parent, which precedes it, every
+ * triangle lies inside its leaf's box, and the tree is at most 94 levels
+ * deep. */
+int nr_scene_create_bvh(const nr_scene_desc* desc, const nr_bvh* bvh, const char* options, nr_scene** out);
+
 /* BVH in depth-first order (left child first): box[6] per node (min, max),
  * kids[2] (-1, -1 for a leaf), leaf_first/leaf_count into leaf_tris
  * (triangle indices in loader order). Returns NR_OK and writes the node count

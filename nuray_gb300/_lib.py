@@ -45,6 +45,11 @@ class Camera(ctypes.Structure):
                 ("fov", ctypes.c_float), ("aspect", ctypes.c_float)]
 
 
+class BvhDesc(ctypes.Structure):
+    _fields_ = [("num_nodes", ctypes.c_int32), ("box", ctypes.c_void_p), ("kids", ctypes.c_void_p),
+                ("leaf_first", ctypes.c_void_p), ("leaf_count", ctypes.c_void_p), ("leaf_tris", ctypes.c_void_p)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("paths", "rays", "shadow_rays", "waves", "bounces", "kernel_launches",
                                                 "trace_launches", "nodes_visited", "tris_tested",
@@ -67,6 +72,7 @@ SIGNATURES = {
     "nr_scene_info": [_vp, _vp],
     "nr_scene_export": [_vp, _vp, _vp, _vp, _vp, _vp],
     "nr_bvh_export": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "nr_scene_create_bvh": [_vp, _vp, _cp, _vp],
     "nr_intersect": [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i32],
     "nr_camera_from_params": [_cp, _vp],
     "nr_render": [_vp, _vp, _cp, _vp, _vp, _vp, _vp, _vp],
@@ -134,9 +140,12 @@ class Scene:
         return cls(h.value)
 
     @classmethod
-    def from_arrays(cls, pos, mat, mats, uv=None, nrm=None, textures=(), env_tex=-1, env_gain=1.0, options=""):
+    def from_arrays(cls, pos, mat, mats, uv=None, nrm=None, textures=(), env_tex=-1, env_gain=1.0, options="",
+                    bvh=None):
         """pos (n,9) float32, mat (n,) int32, mats: list of dicts / Material,
-        textures: list of (h, w, 3) float32 arrays (row 0 at v = 1)."""
+        textures: list of (h, w, 3) float32 arrays (row 0 at v = 1); bvh: a
+        tree (box, kids, first, count, tris) as Scene.bvh() returns it, used
+        instead of a build (nr_scene_create_bvh)."""
         pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 9)
         n = pos.shape[0]
         mat = np.ascontiguousarray(mat, np.int32).reshape(n)
@@ -151,7 +160,13 @@ class Scene:
         d = SceneDesc(n, _ptr(pos), _ptr(uv), _ptr(nrm), _ptr(mat), len(mats), ctypes.addressof(mt), len(textures),
                       _ptr(wh) if len(textures) else None, _ptr(td) if len(textures) else None, env_tex, env_gain)
         h = ctypes.c_void_p()
-        check(lib().nr_scene_create_opts(ctypes.byref(d), options.encode(), ctypes.byref(h)))
+        if bvh is None:
+            check(lib().nr_scene_create_opts(ctypes.byref(d), options.encode(), ctypes.byref(h)))
+        else:
+            box, kids, first, count, tris = (np.ascontiguousarray(a, t) for a, t in
+                                             zip(bvh, (np.float32, np.int32, np.int32, np.int32, np.int32)))
+            tree = BvhDesc(len(kids), _ptr(box), _ptr(kids), _ptr(first), _ptr(count), _ptr(tris))
+            check(lib().nr_scene_create_bvh(ctypes.byref(d), ctypes.byref(tree), options.encode(), ctypes.byref(h)))
         return cls(h.value)
 
     def build_times(self):

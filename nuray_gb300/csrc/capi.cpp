@@ -404,7 +404,7 @@ void upload_scene(nr_scene* s) {
     }
 }
 
-void finish_scene(nr_scene* s, const char* options) {
+void finish_scene(nr_scene* s, const char* options, nr::Bvh* prebuilt = nullptr) {
     const nr::Config opt(options ? options : "");
     const std::string bvh = opt.get_str("bvh");
     if (!bvh.empty() && bvh != "host" && bvh != "gpu") throw NrError(NR_ERR_INVALID, "bvh must be host or gpu");
@@ -424,7 +424,9 @@ void finish_scene(nr_scene* s, const char* options) {
     s->bvh_device_ms = 0.0;
     // the deepest tree the traversal stacks hold; the builders stop past it
     const int depth_limit = NR_STACK_LIMIT - 2;
-    if (bvh == "gpu") {
+    if (prebuilt) {
+        s->bvh = std::move(*prebuilt);
+    } else if (bvh == "gpu") {
         std::string err = nr::build_bvh_gpu(s->host.pos.data(), s->host.num_tris(), s->bvh, s->stream, &s->bvh_device_ms,
                                             depth_limit);
         if (!err.empty()) throw NrError(NR_ERR_CUDA, err);
@@ -1105,6 +1107,22 @@ int nr_scene_create_opts(const nr_scene_desc* desc, const char* options, nr_scen
 }
 
 int nr_scene_create(const nr_scene_desc* desc, nr_scene** out) { return nr_scene_create_opts(desc, nullptr, out); }
+
+int nr_scene_create_bvh(const nr_scene_desc* desc, const nr_bvh* bvh, const char* options, nr_scene** out) {
+    return guarded([&]() {
+        if (!desc || !bvh || !out) throw NrError(NR_ERR_INVALID, "null argument");
+        *out = nullptr;
+        auto s = std::make_unique<nr_scene>();
+        std::string err = nr::scene_from_desc(*desc, s->host);
+        if (!err.empty()) throw NrError(NR_ERR_INVALID, err);
+        nr::Bvh tree;
+        err = nr::bvh_from_arrays(s->host, bvh->num_nodes, bvh->box, bvh->kids, bvh->leaf_first, bvh->leaf_count,
+                                  bvh->leaf_tris, s->host.num_tris(), NR_STACK_LIMIT - 2, tree);
+        if (!err.empty()) throw NrError(NR_ERR_INVALID, "bvh: " + err);
+        finish_scene(s.get(), options, &tree);
+        *out = s.release();
+    });
+}
 
 int nr_scene_load_opts(const char* text, const char* options, nr_scene** out) {
     return guarded([&]() {

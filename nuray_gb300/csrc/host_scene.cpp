@@ -682,6 +682,75 @@ void build_bvh(const HostScene& s, Bvh& out, int threads, int depth_limit) {
     root.reset();
 }
 
+std::string bvh_from_arrays(const HostScene& s, int num_nodes, const float* box, const int32_t* kids,
+                            const int32_t* leaf_first, const int32_t* leaf_count, const int32_t* leaf_tris,
+                            int num_leaf_tris, int depth_limit, Bvh& out) {
+    out = Bvh();
+    const int n = s.num_tris();
+    if (num_nodes < 0 || num_leaf_tris != n) return "the tree must order every triangle once (num_leaf_tris)";
+    if (n == 0) return num_nodes == 0 ? "" : "a tree over no triangles must have no nodes";
+    if (num_nodes < 1 || !box || !kids || !leaf_first || !leaf_count || !leaf_tris) return "tree arrays missing";
+    std::vector<uint8_t> seen((size_t)n, 0);
+    for (int i = 0; i < n; ++i) {
+        const int32_t t = leaf_tris[i];
+        if (t < 0 || t >= n || seen[t]++) return "leaf_tris is not a permutation of the triangles";
+    }
+    std::vector<int32_t> parent((size_t)num_nodes, -1);
+    std::vector<uint8_t> covered((size_t)n, 0);
+    out.nodes.resize((size_t)num_nodes);
+    for (int i = 0; i < num_nodes; ++i) {
+        BvhNode& nd = out.nodes[i];
+        for (int k = 0; k < 3; ++k) {
+            nd.lo[k] = box[6 * (size_t)i + k];
+            nd.hi[k] = box[6 * (size_t)i + 3 + k];
+            if (!std::isfinite(nd.lo[k]) || !std::isfinite(nd.hi[k]) || nd.lo[k] > nd.hi[k])
+                return "node " + std::to_string(i) + ": bad box";
+        }
+        nd.left = kids[2 * (size_t)i];
+        nd.right = kids[2 * (size_t)i + 1];
+        nd.first = nd.count = 0;
+        if (nd.left < 0 || nd.right < 0) {
+            if (nd.left != -1 || nd.right != -1) return "node " + std::to_string(i) + ": a leaf has kids -1, -1";
+            nd.first = leaf_first[i];
+            nd.count = leaf_count[i];
+            // the device encodes a leaf's count in 3 bits
+            if (nd.count < 0 || nd.count > 7 || nd.first < 0 || (int64_t)nd.first + nd.count > n)
+                return "node " + std::to_string(i) + ": leaf range outside the triangles (at most 7 per leaf)";
+            for (int j = nd.first; j < nd.first + nd.count; ++j) {
+                if (covered[j]++) return "leaves overlap at triangle position " + std::to_string(j);
+                const float* p = &s.pos[9 * (size_t)leaf_tris[j]];
+                for (int v = 0; v < 3; ++v)
+                    for (int k = 0; k < 3; ++k)
+                        if (!(p[3 * v + k] >= nd.lo[k] && p[3 * v + k] <= nd.hi[k]))
+                            return "node " + std::to_string(i) + ": its box does not hold triangle " +
+                                   std::to_string(leaf_tris[j]);
+            }
+        } else {
+            for (int32_t c : {nd.left, nd.right}) {
+                if (c <= i || c >= num_nodes) return "node " + std::to_string(i) + ": a child must follow its parent";
+                if (parent[c] >= 0) return "node " + std::to_string(c) + " has two parents";
+                parent[c] = i;
+            }
+        }
+    }
+    for (int j = 0; j < n; ++j)
+        if (!covered[j]) return "triangle position " + std::to_string(j) + " is in no leaf";
+    // every node but the root has its parent before it: depths in one pass
+    out.nodes[0].depth = 0;
+    for (int i = 1; i < num_nodes; ++i) {
+        if (parent[i] < 0) return "node " + std::to_string(i) + " is not reachable from the root";
+        out.nodes[i].depth = out.nodes[parent[i]].depth + 1;
+        out.max_depth = std::max(out.max_depth, out.nodes[i].depth);
+        if (out.max_depth > depth_limit) {
+            out = Bvh();
+            out.max_depth = depth_limit + 1;
+            return "";
+        }
+    }
+    out.leaf_tris.assign(leaf_tris, leaf_tris + n);
+    return "";
+}
+
 std::string check_tree_refs(const int32_t* refs, int num_inner, int num_tris) {
     std::vector<uint8_t> referenced((size_t)std::max(num_inner, 0), 0);
     for (int i = 0; i < num_inner; ++i)

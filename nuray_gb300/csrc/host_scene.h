@@ -99,6 +99,17 @@ struct Bvh {
 // recursing as deep as the scene asks (identical triangles make a chain).
 void build_bvh(const HostScene& s, Bvh& out, int threads, int depth_limit = 2048);
 
+// A tree given by the caller in the layout of nr_bvh_export (box[6] per
+// node, kids[2] with -1, -1 for a leaf, leaf_first / leaf_count into
+// leaf_tris, the triangle order in loader indices) over the triangles of s,
+// checked and turned into out: node 0 is the root; every other node is the
+// child of exactly one node, which precedes it; leaves partition leaf_tris,
+// which is a permutation of the triangles; every triangle lies inside its
+// leaf's box; the depth is at most depth_limit. Returns "" or what is wrong.
+std::string bvh_from_arrays(const HostScene& s, int num_nodes, const float* box, const int32_t* kids,
+                            const int32_t* leaf_first, const int32_t* leaf_count, const int32_t* leaf_tris,
+                            int num_leaf_tris, int depth_limit, Bvh& out);
+
 // The shape the device traversal relies on, checked on the child references
 // of the GPU node array (two per inner node: >= 0 an inner node, < 0 a leaf
 // -1 - ((first << 3) | count)): every inner node is the child of at most one

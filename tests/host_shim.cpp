@@ -105,6 +105,22 @@ int shim_read_image(const char* path, int* w, int* h, float* rgb, char* err, int
     return 0;
 }
 
+// nr::bvh_from_arrays over n triangles: 0 (depth in *depth), or -1 with the message.
+int shim_bvh_from_arrays(int n, const float* pos, int num_nodes, const float* box, const int32_t* kids,
+                         const int32_t* first, const int32_t* count, const int32_t* tris, int depth_limit, int* depth,
+                         char* err, int errlen) {
+    nr::HostScene s;
+    s.pos.assign(pos, pos + 9 * (size_t)n);
+    s.mat.assign(n, 0);
+    nr::Bvh b;
+    std::string e = nr::bvh_from_arrays(s, num_nodes, box, kids, first, count, tris, n, depth_limit, b);
+    if (depth) *depth = b.max_depth;
+    if (e.empty()) return 0;
+    std::strncpy(err, e.c_str(), (size_t)errlen - 1);
+    err[errlen - 1] = 0;
+    return -1;
+}
+
 // nr::check_tree_refs: 0 for a tree the traversal accepts, -1 with the message.
 int shim_check_tree(const int32_t* refs, int num_inner, int num_tris, char* err, int errlen) {
     std::string e = nr::check_tree_refs(refs, num_inner, num_tris);

@@ -35,6 +35,8 @@ def load():
     L.shim_png_encode.restype = ctypes.c_long
     L.shim_read_image.argtypes = [ctypes.c_char_p, vp, vp, vp, ctypes.c_char_p, ctypes.c_int]
     L.shim_check_tree.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+    L.shim_bvh_from_arrays.argtypes = [ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_int, vp,
+                                       ctypes.c_char_p, ctypes.c_int]
     return L
 
 
@@ -108,3 +110,16 @@ def load_scene(L, desc):
     L.shim_load(desc.encode(), pos.ctypes.data, uv.ctypes.data, nrm.ctypes.data, mat.ctypes.data,
                 ctypes.addressof(mats), ctypes.byref(nm), err, 512)
     return pos, uv, nrm, mat, [mats[i] for i in range(nm.value)]
+
+
+def bvh_from_arrays(L, pos, tree, depth_limit=94):
+    """nr::bvh_from_arrays on (box, kids, first, count, tris): (0, depth) or (-1, message)."""
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 9)
+    box, kids, first, count, tris = (np.ascontiguousarray(a, t) for a, t in
+                                     zip(tree, (np.float32, np.int32, np.int32, np.int32, np.int32)))
+    depth = ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    rc = L.shim_bvh_from_arrays(len(pos), pos.ctypes.data, len(kids), box.ctypes.data, kids.ctypes.data,
+                                first.ctypes.data, count.ctypes.data, tris.ctypes.data, depth_limit,
+                                ctypes.byref(depth), err, 256)
+    return (0, depth.value) if rc == 0 else (-1, err.value.decode())

@@ -146,3 +146,49 @@ def test_coincident_triangles_are_refused_at_the_depth_limit(gpu_lib):
     S = Scene.from_arrays(pos[:50], np.zeros(50, np.int32), [dict(type=0, c0=(0.5, 0.5, 0.5))], options="bvh=gpu")
     tri = S.intersect(np.float32([[0.2, 0.2, 1.0]]), np.float32([[0, 0, -1]]))[0]
     assert 0 <= tri[0] < 50
+
+
+def test_given_tree_gives_the_same_hits_and_image(gpu_lib):
+    """nr_scene_create_bvh: the tree exported from one scene, handed to a
+    second scene over the same triangles, in depth-first and in
+    breadth-first node order, gives the same closest hits and the same image
+    bit for bit; broken trees are refused."""
+    from nuray_gb300 import Scene, scenes
+    from nuray_gb300._lib import NuRayError
+    sc = scenes.terrain_spheres(2, tiles=16, cells_per_tile=8, spheres=32, slices=16, stacks=12, lights=8, n_mats=8,
+                                extent=64.0)
+    args = (sc["pos"], sc["mat"], sc["mats"])
+    kw = dict(uv=sc["uv"], nrm=sc["nrm"])
+    H = Scene.from_arrays(*args, **kw)
+    box, kids, first, count, tris = H.bvh()
+    order, q = [], [0]
+    while q:
+        v = q.pop(0)
+        order.append(v)
+        if kids[v, 0] >= 0:
+            q += [int(kids[v, 0]), int(kids[v, 1])]
+    new = {old: i for i, old in enumerate(order)}
+    kb = np.array([[new[a], new[b]] if a >= 0 else [-1, -1] for a, b in kids[order]], np.int32)
+    bfs = (box[order], kb, first[order], count[order], tris)
+    rng = np.random.default_rng(3)
+    o = rng.uniform(-30, 30, (100000, 3)).astype(np.float32)
+    o[:, 1] = rng.uniform(5, 40, 100000)
+    d = rng.normal(size=(100000, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    want = H.intersect(o, d)[:2]
+    params = sc["params"].replace("imgw=1920", "imgw=96").replace("imgh=1080", "imgh=54").replace("spp=64", "spp=4")
+    img = H.render(params)
+    for tree in ((box, kids, first, count, tris), bfs):
+        G = Scene.from_arrays(*args, **kw, bvh=tree)
+        got = G.intersect(o, d)[:2]
+        np.testing.assert_array_equal(got[0], want[0])
+        np.testing.assert_array_equal(got[1], want[1])
+        np.testing.assert_array_equal(G.render(params), img)
+    bad = kids.copy()
+    bad[int(np.flatnonzero(kids[:, 0] >= 0)[2]), 0] = 0
+    with pytest.raises(NuRayError, match="NR_ERR_INVALID: bvh: .*follow its parent"):
+        Scene.from_arrays(*args, **kw, bvh=(box, bad, first, count, tris))
+    small = box.copy()
+    small[int(np.flatnonzero(kids[:, 0] < 0)[0]), 3:] = small[int(np.flatnonzero(kids[:, 0] < 0)[0]), :3]
+    with pytest.raises(NuRayError, match="does not hold"):
+        Scene.from_arrays(*args, **kw, bvh=(small, kids, first, count, tris))

@@ -158,6 +158,50 @@ def test_bvh_builder_stops_at_its_depth_limit(host):
     assert depth == 55 and len(kids) == 2 * 55 + 1  # a chain within the limit is built whole
 
 
+def test_given_trees_are_checked_before_use(host):
+    """nr_scene_create_bvh's check (nr::bvh_from_arrays) on the builder's own
+    tree, the same tree in breadth-first order (children still after their
+    parents), and trees broken one way at a time."""
+    sc = scenes.terrain_spheres(3, tiles=8, cells_per_tile=8, spheres=16, slices=12, stacks=8, lights=4,
+                                n_mats=4, extent=32.0)
+    pos = sc["pos"]
+    box, kids, first, count, tris, depth = shim.bvh(host, pos)
+    tree = (box, kids, first, count, tris)
+    assert shim.bvh_from_arrays(host, pos, tree) == (0, depth)
+    # breadth-first order of the same nodes
+    order, q = [], [0]
+    while q:
+        v = q.pop(0)
+        order.append(v)
+        if kids[v, 0] >= 0:
+            q += [int(kids[v, 0]), int(kids[v, 1])]
+    new = {old: i for i, old in enumerate(order)}
+    kb = np.array([[new[a], new[b]] if a >= 0 else [-1, -1] for a, b in kids[order]], np.int32)
+    assert shim.bvh_from_arrays(host, pos, (box[order], kb, first[order], count[order], tris)) == (0, depth)
+    assert shim.bvh_from_arrays(host, pos, tree, depth_limit=3) == (0, 4)  # too deep: no tree, depth past the limit
+
+    def broken(edit):
+        t = [a.copy() for a in tree]
+        edit(t)
+        return shim.bvh_from_arrays(host, pos, t)
+
+    leaf = int(np.flatnonzero(kids[:, 0] < 0)[3])
+    inner = int(np.flatnonzero(kids[:, 0] >= 0)[5])
+
+    def dup_tri(t): t[4][1] = t[4][0]
+    def child_first(t): t[1][inner, 0] = 0
+    def two_parents(t): t[1][inner, 1] = t[1][inner, 0]
+    def box_too_small(t): t[0][leaf, 3:] = t[0][leaf, :3]
+    def overlap(t): t[2][leaf] = t[2][leaf] - 1 if t[2][leaf] > 0 else t[2][leaf] + 1
+    def nan_box(t): t[0][inner, 0] = np.nan
+    def big_leaf(t): t[3][leaf] = 8
+    for edit, msg in ((dup_tri, "permutation"), (child_first, "follow its parent"), (two_parents, "two parents"),
+                      (box_too_small, "does not hold"), (overlap, "overlap"), (nan_box, "bad box"),
+                      (big_leaf, "at most 7")):
+        rc, m = broken(edit)
+        assert rc == -1 and msg in m, (edit.__name__, m)
+
+
 def test_image_headers_promising_more_than_the_file_holds_are_refused(host, tmp_path):
     """Declared sizes are checked against the data before anything is
     allocated for the pixels: PPM and PFM against the bytes left in the
