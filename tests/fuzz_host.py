@@ -2,8 +2,9 @@
 shim (tests/host_shim.cpp): PNG (with repaired chunk CRCs, so corrupted
 deflate streams reach the inflater), JPEG (baseline, progressive, restart
 intervals, subsampled, non-interleaved), OBJ/MTL scene descriptions and the
-key=value parameter grammar. Each input must decode or be refused; nothing
-may crash. Run as a child process by tests/test_fuzz_host.py:
+key=value parameter grammar, and trees handed to nr_scene_create_bvh. Each
+input must decode or be refused; nothing may crash. Run as a child process
+by tests/test_fuzz_host.py:
 
     python tests/fuzz_host.py KIND FIRST COUNT
 
@@ -162,6 +163,30 @@ def obj_case(folder, idx):
     return desc + "\n"
 
 
+def _tree_seed(L):
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(-5, 5, (300, 9)).astype(np.float32)
+    box, kids, first, count, tris, _ = shim.bvh(L, pos)
+    return pos, (box, kids, first, count, tris)
+
+
+def tree_case(tree, idx):
+    """The builder's tree with a few entries of its arrays set to values in and
+    out of range (the arrays keep their lengths, as the API requires)."""
+    rng = np.random.default_rng(idx)
+    t = [a.copy() for a in tree]
+    n_nodes, n = len(t[1]), len(t[4])
+    for _ in range(rng.integers(1, 4)):
+        which = rng.integers(0, 5)
+        a = t[which].reshape(-1)
+        i = rng.integers(0, len(a))
+        if which == 0:
+            a[i] = [np.nan, np.inf, -np.inf, 0.0, 1e30, -1e30, a[i] * 0.5][rng.integers(0, 7)]
+        else:
+            a[i] = [-1, -2, 0, 1, n_nodes - 1, n_nodes, n - 1, n, 7, 8, 2 ** 31 - 1, -2 ** 31][rng.integers(0, 12)]
+    return t
+
+
 PARAM_TOKENS = ["imgw=", "spp=", "campos=", "cameuler=", "camfov=", "=", "==", "1", "-1", "1e40", "nan", "inf", ",",
                 ",,", "1,2", "1,2,3,4", " ", "\t", "a=b=c", "x", "99999999999999999999", "-0", "0x1f", "1e-50"]
 
@@ -192,6 +217,10 @@ def main():
                 shim.load_scene(L, obj_case(folder, i))
             except (ValueError, MemoryError):
                 pass
+    elif kind == "tree":
+        pos, tree = _tree_seed(L)
+        for i in range(first, first + count):
+            shim.bvh_from_arrays(L, pos, tree_case(tree, i))
     elif kind == "params":
         out = (ctypes.c_float * 3)()
         cam = (ctypes.c_float * 11)()  # nr_camera
