@@ -214,8 +214,8 @@ typedef struct nr_bvh {
  * over, or a tree exported earlier). Refused with NR_ERR_INVALID unless
  * leaf_tris is a permutation of the triangles, the leaves partition it,
  * every node but the root has exactly one parent, which precedes it, every
- * triangle lies inside its leaf's box, and the tree is at most 94 levels
- * deep. */
+ * box lies inside its parent's and every triangle inside its leaf's, and
+ * the tree is at most 94 levels deep. */
 int nr_scene_create_bvh(const nr_scene_desc* desc, const nr_bvh* bvh, const char* options, nr_scene** out);
 
 /* BVH in depth-first order (left child first): box[6] per node (min, max),

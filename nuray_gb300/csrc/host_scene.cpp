@@ -735,6 +735,13 @@ std::string bvh_from_arrays(const HostScene& s, int num_nodes, const float* box,
     }
     for (int j = 0; j < n; ++j)
         if (!covered[j]) return "triangle position " + std::to_string(j) + " is in no leaf";
+    // a walk tests a child's box only inside its parent's: boxes must nest
+    for (int i = 1; i < num_nodes; ++i) {
+        const BvhNode &c = out.nodes[i], &p = out.nodes[parent[i] < 0 ? 0 : parent[i]];
+        for (int k = 0; k < 3; ++k)
+            if (parent[i] >= 0 && (c.lo[k] < p.lo[k] || c.hi[k] > p.hi[k]))
+                return "node " + std::to_string(i) + ": its box is not inside its parent's";
+    }
     // every node but the root has its parent before it: depths in one pass
     out.nodes[0].depth = 0;
     for (int i = 1; i < num_nodes; ++i) {

@@ -195,9 +195,10 @@ def test_given_trees_are_checked_before_use(host):
     def overlap(t): t[2][leaf] = t[2][leaf] - 1 if t[2][leaf] > 0 else t[2][leaf] + 1
     def nan_box(t): t[0][inner, 0] = np.nan
     def big_leaf(t): t[3][leaf] = 8
+    def outside_parent(t): t[0][int(t[1][inner, 0]), :3] -= 1.0  # a child box reaching out of its parent's
     for edit, msg in ((dup_tri, "permutation"), (child_first, "follow its parent"), (two_parents, "two parents"),
                       (box_too_small, "does not hold"), (overlap, "overlap"), (nan_box, "bad box"),
-                      (big_leaf, "at most 7")):
+                      (big_leaf, "at most 7"), (outside_parent, "inside its parent")):
         rc, m = broken(edit)
         assert rc == -1 and msg in m, (edit.__name__, m)
 
