@@ -306,7 +306,8 @@ int nr_intersect_noalloc(nr_scene* scene, int32_t n, const float* o, const float
  * image where a material's pdf() is its sampling density, as for Lambert, but
  * not on GGX-reflect, whose pdf() omits the half-vector Jacobian),
  * profile=1 and count=1 (see nr_stats). cam may be NULL to take the camera from
- * params. hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
+ * params; a camera with a non-finite value, a fov outside (0, 180) degrees
+ * or a non-positive aspect is refused (NR_ERR_INVALID). hdr_rgb (W*H*3 floats, the per-pixel mean of max(0, L)) and rgb8
  * (W*H*3 bytes: mean^(1/2.2)*255 clamped and truncated, as
  * src/renderer/rendererptls.cpp:175-180) may each be NULL. cancel, if not
  * NULL, is polled between waves; 0 cancels (the reference's con_flag).
