@@ -393,7 +393,7 @@ int nr_nrc_train_step(nr_nrc* nrc, int32_t n, const float* x, const float* y, fl
  * vertex depth >= nrc_mindepth (default 1), with the cache's prediction, and
  * trains the cache online on the suffix radiance of nrc_train training paths
  * per wavefront batch in nrc_steps Adam steps (defaults: 16384 and 3 for
- * batches of more than 2^22 paths, 8192 and 1 for smaller ones). Training paths end in the cache too, from vertex depth
+ * batches of more than 2^22 paths, 4096 and 1 for smaller ones). Training paths end in the cache too, from vertex depth
  * nrc_train_depth on (default 3; 0 lets them run to the end), as the
  * reference's path_lim_train does (src/renderer/renderernrc.cpp:130). The
  * counts stay on the device: a render with nrc=1 adds no host

@@ -700,16 +700,17 @@ RenderArgs parse_args(const nr_camera* cam, const char* params) {
     // Training work per wave. Waves of more than 2^22 paths (a 1080p frame
     // of 64 spp is one wave) train on 16384 paths in three Adam steps;
     // smaller waves (frames of one or a few samples per pixel, the real-time
-    // regime, where the training's fixed cost weighs on every frame) on 8192
+    // regime, where the training's fixed cost weighs on every frame) on 4096
     // in one step. Time to relMSE 1e-3 against plain PT on the 1M-triangle
     // scene, interpolated to the crossing: 1080p at 64 spp per frame, three
-    // steps 0.89x, two 0.90x; 960x540 at 1 spp per frame, one step and 8192
-    // paths 0.92x, one step 0.94x, two 0.97x, three 1.01x.
+    // steps 0.89x, two 0.90x; 960x540 at 1 spp per frame, one step on 16384
+    // paths 0.94x, on 8192 0.92x (0.98x once the tail kernel had sped plain
+    // PT up), on 4096 0.965x on that same run; two steps 0.97x, three 1.01x.
     {
         const int64_t wave_paths =
             std::min<int64_t>(std::max<int64_t>(0, (int64_t)a.pol.imgw * a.pol.imgh * a.spp), (int64_t)a.wave);
         const bool big_wave = wave_paths > nr::SHADE_SPLIT_MIN;
-        a.nrc_train = c.get_int("nrc_train", big_wave ? 16384 : 8192);
+        a.nrc_train = c.get_int("nrc_train", big_wave ? 16384 : 4096);
         a.nrc_steps = c.get_int("nrc_steps", big_wave ? 3 : 1);
     }
     a.nrc_query = c.get_int("nrc_query", 1);
