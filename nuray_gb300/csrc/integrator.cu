@@ -99,11 +99,12 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 // refilled idle lanes from the queue with separate node and leaf phases,
 // 28 % slower; a four-wide tree collapsed from this one, no faster.)
 // Minimum resident 128-thread blocks per SM requested from the register
-// allocator for the two traversal kernels: 10 caps them at 48 registers
-// (40 warps per SM). Traversal is bound by dependent L2 latency, so the
-// extra warps pay: measured on GB300 for the 1M-triangle frame, 566
-// Mpaths/s at 10 against 530 with no cap (53 registers, 36 warps) and 541
-// at 12 (40 registers, with spills).
+// allocator for the two traversal kernels (NR_TRACE_MINB, NR_SHADOW_MINB
+// below). Traversal is bound by dependent L2 latency, so extra warps pay:
+// measured on GB300 for the 1M-triangle frame with the if-if loops, 566
+// Mpaths/s at 10 blocks (48 registers, 40 warps) against 530 with no cap
+// (53 registers, 36 warps) and 541 at 12 (40 registers, with spills); the
+// current loops and caps below.
 // Loop shape (NR_WW bits): 1 closest hit while-while with postponed leaves
 // (closest_hit_ww), 8 the same without postponing; 2 / 4 any hit likewise;
 // 0 the if-if loops (closest_hit, any_hit). Measured for the 1M-triangle
@@ -134,7 +135,9 @@ __device__ __forceinline__ void warp_count(uint32_t v, uint32_t* lohi) {
 #define NR_WW 5
 #endif
 // Entries of each traversal stack kept in shared memory (a power of two; 0:
-// all in local memory). Measured on the 1M-triangle frame: see DESIGN.
+// all in local memory). Measured on the 1M-triangle frame: K = 4 704.2 and
+// K = 8 706.1 against 757.5 Mpaths/s with the whole stack in local memory
+// (L1-resident already; the ring's index arithmetic costs issue slots).
 #ifndef NR_SMEM_STACK
 #define NR_SMEM_STACK 0
 #endif
