@@ -201,7 +201,7 @@ def cpu_leg(sc, params, spp, w, h, stride, budget_s=20.0):
     P = Oracle("port", sc)
     threads = os.cpu_count() or 1
     pix = cpu_sample_pixels(w, h, stride)
-    # calibrate on a small slice, then size the timed sample to the budget
+    # calibrate on a small slice, then size the timed sample to the time target
     probe = pix[:: max(1, len(pix) // 256)]
     t = time.perf_counter()
     P.render_samples(params, probe, spp, threads=threads)

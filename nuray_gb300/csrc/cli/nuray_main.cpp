@@ -91,7 +91,7 @@ int main(int argc, char** argv) {
     nr::Config cfg(params.str().c_str());
     std::string renderer = cfg.get_str("renderer");  // Config::getValueStr returns "" when absent
     if (renderer != "ptnee" && renderer != "pt" && renderer != "nrc") {
-        std::cerr << "renderer=" << renderer << " is not available (this build implements renderer=ptnee, pt and nrc)\n";
+        std::cerr << "renderer=" << renderer << " is not available (this library implements renderer=ptnee, pt and nrc)\n";
         return 2;
     }
     nr_nrc* cache = nullptr;
