@@ -34,6 +34,23 @@ def test_library_exports_every_declared_symbol():
     assert sorted(SIGNATURES) == names
 
 
+def test_header_is_plain_c_and_links_from_c(tmp_path):
+    """The boundary is a C ABI: include/nuray.h parses as pedantic C99, and a C
+    program calling every declared entry point links against the library."""
+    import subprocess
+    from nuray_gb300 import build
+    lib = build.build()
+    names = declared_functions()
+    src = tmp_path / "use.c"
+    calls = "\n".join(f"    if (argc > 99) (void)(size_t)&{n};" for n in names)
+    src.write_text('#include <stddef.h>\n#include "nuray.h"\nint main(int argc, char** argv) {\n    (void)argv;\n'
+                   + calls + "\n    return nr_scene_destroy(NULL) == NR_OK ? 1 : 0;\n}\n")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-L", os.path.dirname(lib), "-lnuray_gpu", "-o", str(tmp_path / "use")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_library_without_gpu_reports_errors():
     import torch
     if torch.cuda.is_available():
